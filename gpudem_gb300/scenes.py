@@ -1,0 +1,317 @@
+"""Seeded synthetic scenes: wall meshes and particle beds.
+
+The reference reads its walls from ASCII STL files (TriangleMesh.cu:363) and
+places particles by O(N^2) rejection sampling (ParticleSystem.cu:219-285).
+Here the same kinds of inputs are generated directly as arrays:
+
+* meshes are ``(T, 3, 3)`` float64 arrays of triangle corners in "file order"
+  (the order an STL file would list them), which is what the mesh ingestion
+  of the engine (and of the reference loader) consumes;
+* particle beds are positions ``(N, 3)`` and radii ``(N,)``, non-overlapping,
+  from a seeded ``numpy.random.Generator``.
+
+Gravity points along -y, as in the reference's shipped cases
+(demSettings.json "gravity": {"y": -9.81}).
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+PI_REF_MASS = 3.14      # main.cu:67 uses 3.14 for the sphere volume
+PI_REF_DAMP = 3.1415    # ParticleSystem.cu:301 uses 3.1415 in the damping constant
+
+
+# --------------------------------------------------------------------------- materials
+
+def sphere_mass(rho: float, r):
+    """m = rho*3.14*r^3*4/3 in the reference's operation order (main.cu:67)."""
+    r = np.asarray(r, dtype=np.float64)
+    return (((((rho * PI_REF_MASS) * r) * r) * r) * 4.0) / 3.0
+
+
+def stiffness_from_E(E: float, r: float) -> float:
+    """k = 4/3*(E/2)*sqrt(r/2)*sqrt(0.05 r) (ParticleSystem.cu:202)."""
+    return 4.0 / 3.0 * (E * 0.5) * math.sqrt(r * 0.5) * math.sqrt(0.05 * r)
+
+
+def eta_const(k, e: float):
+    """etaconst = -2 ln e sqrt(k/(3.1415^2 + ln^2 e)) (ParticleSystem.cu:301)."""
+    k = np.asarray(k, dtype=np.float64)
+    le = math.log(e)
+    return -2.0 * le * np.sqrt(k / (PI_REF_DAMP * PI_REF_DAMP + le * le))
+
+
+# --------------------------------------------------------------------------- meshes
+
+def _quad(a, b, c, d):
+    """Two triangles (a,b,c) and (a,c,d) of a planar quad, in file order."""
+    return [(a, b, c), (a, c, d)]
+
+
+def box_mesh(half=0.1, center=(0.0, 0.0, 0.0)) -> np.ndarray:
+    """Closed axis-aligned cube of side 2*half: 12 triangles."""
+    c = np.asarray(center, dtype=np.float64)
+    h = float(half)
+    p = lambda x, y, z: tuple(c + h * np.array([x, y, z], dtype=np.float64))
+    tris = []
+    tris += _quad(p(1, -1, -1), p(1, 1, -1), p(1, 1, 1), p(1, -1, 1))      # +x
+    tris += _quad(p(1, -1, 1), p(1, 1, 1), p(-1, 1, 1), p(-1, -1, 1))      # +z
+    tris += _quad(p(-1, -1, 1), p(-1, 1, 1), p(-1, 1, -1), p(-1, -1, -1))  # -x
+    tris += _quad(p(-1, -1, -1), p(-1, 1, -1), p(1, 1, -1), p(1, -1, -1))  # -z
+    tris += _quad(p(-1, 1, -1), p(-1, 1, 1), p(1, 1, 1), p(1, 1, -1))      # +y
+    tris += _quad(p(-1, -1, -1), p(1, -1, -1), p(1, -1, 1), p(-1, -1, 1))  # -y
+    return np.asarray(tris, dtype=np.float64)
+
+
+def subdivide(tris: np.ndarray, levels: int) -> np.ndarray:
+    """Split every triangle into 4 (midpoint subdivision), `levels` times."""
+    t = np.asarray(tris, dtype=np.float64)
+    for _ in range(levels):
+        a, b, c = t[:, 0], t[:, 1], t[:, 2]
+        ab, bc, ca = 0.5 * (a + b), 0.5 * (b + c), 0.5 * (c + a)
+        t = np.concatenate([
+            np.stack([a, ab, ca], 1), np.stack([ab, b, bc], 1),
+            np.stack([ca, bc, c], 1), np.stack([ab, bc, ca], 1)], 0)
+    return t
+
+
+def rotate_z(tris: np.ndarray, deg: float) -> np.ndarray:
+    th = math.radians(deg)
+    R = np.array([[math.cos(th), -math.sin(th), 0.0],
+                  [math.sin(th), math.cos(th), 0.0],
+                  [0.0, 0.0, 1.0]])
+    return np.einsum("ij,tcj->tci", R, tris)
+
+
+def tilted_box_mesh(half=0.1, deg=30.0, levels=0) -> np.ndarray:
+    """Closed cube tilted by `deg` about z (like geometry/simpleBox30deg.stl),
+    optionally face-subdivided (12 * 4**levels triangles)."""
+    return rotate_z(subdivide(box_mesh(half), levels), deg)
+
+
+def helical_chute_mesh(radius=0.3, pitch=0.1, turns=2.0, width=0.12, wall=0.05,
+                       n_target=50_000, seed=3) -> np.ndarray:
+    """Parametric helical chute: a ramp winding around the y axis plus an outer
+    side wall, tessellated to about `n_target` triangles.  The ramp surface
+    spans radii [radius-width, radius]; the wall stands `wall` high at the
+    outer radius.  A seeded +-2 % jitter of the ramp's radial samples keeps the
+    triangles from being perfectly regular."""
+    rng = np.random.default_rng(seed)
+    n_r = 6                                   # radial quads on the ramp
+    n_h = 3                                   # vertical quads on the outer wall
+    per_step = 2 * (n_r + n_h)
+    n_t = max(4, int(round(n_target / per_step)))
+    th = np.linspace(0.0, 2 * math.pi * turns, n_t + 1)
+    y0 = pitch * th / (2 * math.pi)
+    r_in = radius - width
+    rr = np.linspace(r_in, radius, n_r + 1)
+    jit = 1.0 + 0.02 * (rng.random((n_t + 1, n_r + 1)) - 0.5)
+    jit[:, 0] = 1.0
+    jit[:, -1] = 1.0
+    R = rr[None, :] * jit
+    ramp = np.stack([R * np.cos(th)[:, None], np.repeat(-y0[:, None], n_r + 1, 1),
+                     R * np.sin(th)[:, None]], -1)            # descends as theta grows
+    tris = []
+    for a in range(n_t):
+        for b in range(n_r):
+            tris += _quad(ramp[a, b], ramp[a + 1, b], ramp[a + 1, b + 1], ramp[a, b + 1])
+    hh = np.linspace(0.0, wall, n_h + 1)
+    wallp = np.stack([radius * np.repeat(np.cos(th)[:, None], n_h + 1, 1),
+                      -y0[:, None] + hh[None, :],
+                      radius * np.repeat(np.sin(th)[:, None], n_h + 1, 1)], -1)
+    for a in range(n_t):
+        for b in range(n_h):
+            tris += _quad(wallp[a, b], wallp[a + 1, b], wallp[a + 1, b + 1], wallp[a, b + 1])
+    return np.asarray(tris, dtype=np.float64)
+
+
+def corrugated_floor_mesh(length=1.0, width=0.2, amp=0.003, n_target=200_000, seed=5) -> np.ndarray:
+    """Floor of a channel along x with seeded sinusoidal bumps of amplitude
+    `amp`, triangulated to about `n_target` triangles (a regular grid of quads)."""
+    rng = np.random.default_rng(seed)
+    nx = int(math.sqrt(n_target / 2 * length / width))
+    nz = max(1, int(n_target / 2 / nx))
+    x = np.linspace(-0.5 * length, 0.5 * length, nx + 1)
+    z = np.linspace(-0.5 * width, 0.5 * width, nz + 1)
+    X, Z = np.meshgrid(x, z, indexing="ij")
+    k1, k2 = rng.uniform(20, 60, 2)
+    p1, p2 = rng.uniform(0, 2 * math.pi, 2)
+    Y = amp * np.sin(k1 * X + p1) * np.cos(k2 * Z + p2)
+    P = np.stack([X, Y, Z], -1)
+    a = P[:-1, :-1].reshape(-1, 3)
+    b = P[1:, :-1].reshape(-1, 3)
+    c = P[1:, 1:].reshape(-1, 3)
+    d = P[:-1, 1:].reshape(-1, 3)
+    t1 = np.stack([a, b, c], 1)
+    t2 = np.stack([a, c, d], 1)
+    return np.concatenate([t1, t2], 0)
+
+
+# --------------------------------------------------------------------------- particles
+
+def random_packing(n, radii, lo, hi, rng, max_trials=2000):
+    """Seeded random sequential addition of non-overlapping spheres inside the
+    axis-aligned region [lo, hi] (centres kept r away from the faces), with a
+    uniform hash grid so it runs in O(N).  Raises if a sphere cannot be placed
+    (like ParticleSystem.cu:282)."""
+    radii = np.asarray(radii, dtype=np.float64)
+    lo = np.asarray(lo, dtype=np.float64)
+    hi = np.asarray(hi, dtype=np.float64)
+    rmax = float(radii.max())
+    cell = 2.0 * rmax
+    dims = np.maximum(1, np.ceil((hi - lo) / cell).astype(np.int64))
+    grid: dict = {}
+    pos = np.zeros((n, 3))
+    for i in range(n):
+        r = radii[i]
+        placed = False
+        for _ in range(max_trials):
+            p = lo + r + rng.random(3) * (hi - lo - 2 * r)
+            c = np.minimum(((p - lo) / cell).astype(np.int64), dims - 1)
+            ok = True
+            for dx in (-1, 0, 1):
+                for dy in (-1, 0, 1):
+                    for dz in (-1, 0, 1):
+                        for j in grid.get((c[0] + dx, c[1] + dy, c[2] + dz), ()):
+                            d = p - pos[j]
+                            if d @ d < (r + radii[j]) ** 2:
+                                ok = False
+                                break
+                        if not ok:
+                            break
+                    if not ok:
+                        break
+                if not ok:
+                    break
+            if ok:
+                pos[i] = p
+                grid.setdefault((c[0], c[1], c[2]), []).append(i)
+                placed = True
+                break
+        if not placed:
+            raise RuntimeError(f"could not place particle {i} of {n}")
+    return pos
+
+
+def lattice_packing(n, radii, lo, hi, rng, gap=0.1):
+    """Jittered simple-cubic lattice fill of [lo, hi] (fast for millions):
+    spacing 2*rmax*(1+gap), each centre jittered by up to gap*rmax, so spheres
+    never overlap.  Lattice sites are taken in a seeded random order."""
+    radii = np.asarray(radii, dtype=np.float64)
+    lo = np.asarray(lo, dtype=np.float64)
+    hi = np.asarray(hi, dtype=np.float64)
+    rmax = float(radii.max())
+    a = 2.0 * rmax * (1.0 + gap)
+    dims = np.floor((hi - lo - 2 * rmax) / a).astype(np.int64) + 1
+    total = int(np.prod(dims))
+    if total < n:
+        raise RuntimeError(f"lattice region holds {total} < {n} spheres")
+    sites = rng.permutation(total)[:n]
+    iz = sites % dims[2]
+    iy = (sites // dims[2]) % dims[1]
+    ix = sites // (dims[1] * dims[2])
+    base = lo + rmax + np.stack([ix, iy, iz], 1) * a
+    jit = (rng.random((n, 3)) - 0.5) * (gap * rmax)
+    return base + jit
+
+
+@dataclass
+class Scene:
+    """Everything a step engine needs for one scene (SI units, reference layout)."""
+    x: np.ndarray            # (N,3) positions
+    r: np.ndarray            # (N,)
+    m: np.ndarray            # (N,)
+    k: np.ndarray            # (N,) normal = tangential stiffness (linear model)
+    eta: np.ndarray          # (N,) damping constant (etaconst)
+    mu: float
+    dt: float
+    tris: np.ndarray         # (T,3,3) file-order triangles
+    inlet_lo: np.ndarray     # region the box limits must contain (BoundingBox.cu:448)
+    inlet_hi: np.ndarray
+    g: np.ndarray = field(default_factory=lambda: np.array([0.0, -9.81, 0.0]))
+    v: np.ndarray | None = None
+    w: np.ndarray | None = None
+    skin: float = -1.0       # <= 0 keeps the reference default (r_max)
+    refresh: float = -1.0
+    # Hertz-Mindlin material (used when the engine runs the HM model)
+    E: float = 0.0
+    nu: float = 0.0
+    e: float = 0.5
+    mu_roll: float = 0.0
+    name: str = ""
+
+    @property
+    def n(self) -> int:
+        return int(self.x.shape[0])
+
+
+def config1_box_drop(n=100, seed=1) -> Scene:
+    """100 monodisperse spheres (r=0.01 m, rho=2500) at seeded non-overlapping
+    positions in the upper half of a closed 0.2 m box (12 triangles); linear
+    spring-dashpot kn=1e5 N/m, restitution 0.5, mu=0.5, dt=1e-5 s, Verlet
+    skin 0.1 r."""
+    rng = np.random.default_rng(seed)
+    r0 = 0.01
+    radii = np.full(n, r0)
+    half = 0.1
+    x = random_packing(n, radii, [-half, 0.0, -half], [half, half, half], rng)
+    m = sphere_mass(2500.0, radii)
+    k = np.full(n, 1e5)
+    return Scene(x=x, r=radii, m=m, k=k, eta=eta_const(k, 0.5), mu=0.5, dt=1e-5,
+                 tris=box_mesh(half), inlet_lo=np.array([-half, 0.0, -half]),
+                 inlet_hi=np.array([half, half, half]), skin=0.1 * r0, refresh=0.05 * r0,
+                 e=0.5, name="box-drop-100")
+
+
+def config2_tilted_box(n=30_000, seed=2, r0=2e-3, half=0.1, levels=0, linear_k=None) -> Scene:
+    """Spheres with r ~ U[0.8,1.2]*r0 at seeded random packing in the upper part
+    of a closed box tilted 30 degrees (12 triangles).  The Hertz-Mindlin
+    material is E=5e6 Pa, nu=0.3, e=0.6, mu=0.4, dt=2e-6 s; `linear_k` (or the
+    reference's k(E, r0) law) gives the linear-model twin."""
+    rng = np.random.default_rng(seed)
+    radii = r0 * rng.uniform(0.8, 1.2, n)
+    # the tilted cube of half-width `half` contains the axis-aligned cube of
+    # half-width half/(cos30+sin30) around its centre
+    s = half / (math.cos(math.radians(30)) + math.sin(math.radians(30)))
+    lo = np.array([-s, -0.2 * s, -s])
+    hi = np.array([s, s, s])
+    x = lattice_packing(n, radii, lo, hi, rng, gap=0.05) if n > 5000 else \
+        random_packing(n, radii, lo, hi, rng)
+    m = sphere_mass(2500.0, radii)
+    kk = stiffness_from_E(5e6, r0) if linear_k is None else linear_k
+    k = np.full(n, kk)
+    return Scene(x=x, r=radii, m=m, k=k, eta=eta_const(k, 0.6), mu=0.4, dt=2e-6,
+                 tris=tilted_box_mesh(half, 30.0, levels), inlet_lo=lo, inlet_hi=hi,
+                 E=5e6, nu=0.3, e=0.6, name=f"tilted-box-{n}")
+
+
+def lognormal_radii(n, rng, median=1e-3, sigma=0.15, lo=0.6e-3, hi=1.6e-3):
+    r = median * np.exp(sigma * rng.standard_normal(n))
+    return np.clip(r, lo, hi)
+
+
+def config3_helical_chute(n=1_000_000, seed=3, n_tri=50_000) -> Scene:
+    """1e6 lognormal spheres (median 1 mm, sigma_log 0.15, clipped [0.6,1.6] mm)
+    above a seeded helical chute (radius 0.3 m, pitch 0.1 m, ~5e4 triangles),
+    released from a lattice in an annular-sector inlet over the ramp.  HM
+    material E=5e6, nu=0.3, e=0.5, mu=0.5; dt=1e-6 s."""
+    rng = np.random.default_rng(seed)
+    radii = lognormal_radii(n, rng)
+    tris = helical_chute_mesh(n_target=n_tri, seed=seed)
+    # inlet: a box over the start of the ramp, filled as a lattice
+    rmax = float(radii.max())
+    a = 2.0 * rmax * 1.05
+    nx = 40
+    nz = 40
+    ny = int(math.ceil(n / (nx * nz)))
+    lo = np.array([0.3 - 0.12 + 0.004, 0.01, -0.5 * nz * a])
+    hi = lo + np.array([nx * a + 2 * rmax + 1e-9, ny * a + 2 * rmax + 1e-9, nz * a + 2 * rmax + 1e-9])
+    x = lattice_packing(n, radii, lo, hi, rng, gap=0.05)
+    m = sphere_mass(2500.0, radii)
+    k = np.full(n, stiffness_from_E(5e6, 1e-3))
+    return Scene(x=x, r=radii, m=m, k=k, eta=eta_const(k, 0.5), mu=0.5, dt=1e-6,
+                 tris=tris, inlet_lo=lo, inlet_hi=hi, E=5e6, nu=0.3, e=0.5,
+                 name=f"helical-chute-{n}")
