@@ -1,0 +1,122 @@
+"""ctypes binding of the engine's C ABI (include/gdem.h).
+
+The library is the in-tree build gpudem_gb300/_build/libgdem.so.  There is no
+fallback: if it is missing or cannot be loaded, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import _build
+
+GDEM_OK = 0
+ERRORS = {1: "GDEM_ERR_ARG", 2: "GDEM_ERR_CUDA", 3: "GDEM_ERR_CAPACITY", 4: "GDEM_ERR_STATE",
+          5: "GDEM_ERR_RANGE", 6: "GDEM_ERR_DEVICE"}
+FP64, MIXED = 0, 1
+LINEAR, HERTZ_MINDLIN = 0, 1
+
+EXPORTED = [
+    "gdem_create", "gdem_destroy", "gdem_last_error", "gdem_set_mesh", "gdem_import_particles",
+    "gdem_step", "gdem_synchronize", "gdem_export_particles", "gdem_stats_get", "gdem_rebuild",
+    "gdem_export_lists", "gdem_morton_keys", "gdem_export_cells", "gdem_sort_keys",
+    "gdem_dist_triangle", "gdem_export_mesh", "gdem_get_stream", "gdem_profile_step",
+]
+
+
+class Desc(C.Structure):
+    _fields_ = [
+        ("n_particles", C.c_int), ("precision", C.c_int), ("model", C.c_int),
+        ("nei_capacity", C.c_int), ("wall_capacity", C.c_int), ("hist_capacity", C.c_int),
+        ("hist_wall_capacity", C.c_int), ("reorder", C.c_int), ("store_forces", C.c_int),
+        ("steps_per_graph", C.c_int),
+        ("dt", C.c_double), ("mu", C.c_double), ("g", C.c_double * 3),
+        ("box_min", C.c_double * 3), ("box_max", C.c_double * 3),
+        ("cell_size", C.c_double), ("skin", C.c_double), ("refresh_thresh", C.c_double),
+        ("youngs_modulus", C.c_double), ("poisson_ratio", C.c_double),
+        ("restitution", C.c_double), ("rolling_friction", C.c_double),
+    ]
+
+
+_DP = C.POINTER(C.c_double)
+_IP = C.POINTER(C.c_int)
+
+
+class Particles(C.Structure):
+    _fields_ = [
+        ("n", C.c_int), ("x", _DP), ("v", _DP), ("angv", _DP), ("r", _DP), ("m", _DP), ("k", _DP),
+        ("etaconst", _DP), ("isActive", _IP), ("hist_stride", C.c_int), ("numCont", _IP),
+        ("indHis", _IP), ("deltHisx", _DP), ("deltHisy", _DP), ("deltHisz", _DP),
+        ("numContWall", _IP), ("indHisWall", _IP), ("deltHisxWall", _DP), ("deltHisyWall", _DP),
+        ("deltHiszWall", _DP), ("f", _DP), ("mom", _DP),
+    ]
+
+
+class Stats(C.Structure):
+    _fields_ = [
+        ("steps", C.c_longlong), ("rebuilds", C.c_longlong), ("n_active", C.c_longlong),
+        ("n_nei", C.c_longlong), ("n_wall", C.c_longlong), ("n_contacts", C.c_longlong),
+        ("n_wall_contacts", C.c_longlong), ("kinetic_energy", C.c_double),
+        ("coordination", C.c_double), ("packing_fraction", C.c_double),
+        ("max_overlap", C.c_double), ("error_word", C.c_uint), ("max_nei", C.c_int),
+        ("max_wall", C.c_int),
+    ]
+
+
+_lib = None
+
+
+class GdemError(RuntimeError):
+    pass
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = False):
+    """Load libgdem.so; raise if it is absent (no CPU fallback exists)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = lib_path()
+    if not os.path.exists(path):
+        if build_if_missing:
+            _build.build_engine()
+        else:
+            raise GdemError(f"{path} not built: run __graft_entry__.build() (nvcc, sm_103a)")
+    L = C.CDLL(path)
+    vp = C.c_void_p
+    L.gdem_create.argtypes = [C.POINTER(Desc), C.POINTER(vp)]
+    L.gdem_destroy.argtypes = [vp]
+    L.gdem_last_error.argtypes = [vp]
+    L.gdem_last_error.restype = C.c_char_p
+    L.gdem_set_mesh.argtypes = [vp, vp, C.c_int, vp, C.c_int]
+    L.gdem_import_particles.argtypes = [vp, C.POINTER(Particles)]
+    L.gdem_step.argtypes = [vp, C.c_int]
+    L.gdem_synchronize.argtypes = [vp]
+    L.gdem_export_particles.argtypes = [vp, C.POINTER(Particles)]
+    L.gdem_stats_get.argtypes = [vp, C.POINTER(Stats)]
+    L.gdem_rebuild.argtypes = [vp]
+    L.gdem_export_lists.argtypes = [vp, C.c_int, vp, vp, vp, vp]
+    L.gdem_morton_keys.argtypes = [vp, vp]
+    L.gdem_export_cells.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+    L.gdem_sort_keys.argtypes = [vp, C.c_int, vp, vp]
+    L.gdem_dist_triangle.argtypes = [vp, vp, vp, vp, C.c_int, vp, vp]
+    L.gdem_export_mesh.argtypes = [vp, vp, vp, vp, vp, vp]
+    L.gdem_get_stream.argtypes = [vp, C.POINTER(vp)]
+    L.gdem_profile_step.argtypes = [vp, C.c_int, C.POINTER(C.c_float)]
+    for nm in EXPORTED:
+        if nm != "gdem_last_error":
+            getattr(L, nm).restype = C.c_int
+    _lib = L
+    return L
+
+
+def check(rc: int, h=None, what: str = ""):
+    if rc != GDEM_OK:
+        msg = ""
+        if h is not None and _lib is not None:
+            m = _lib.gdem_last_error(h)
+            msg = m.decode() if m else ""
+        raise GdemError(f"{what}: {ERRORS.get(rc, rc)} {msg}".strip())

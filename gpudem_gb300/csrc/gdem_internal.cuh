@@ -1,0 +1,281 @@
+// Internal device-side layout of the GB300 DEM engine.
+//
+// Particle storage is structure-of-arrays with one array per scalar component
+// (x, y, z separately), so a warp of consecutive particles loads 256
+// contiguous bytes per component.  Per-particle rows of variable length
+// (Verlet list, wall list, contact history) are stored "slot-major"
+// (element k of particle i at [k * n + i]): consecutive threads touch
+// consecutive addresses for the same slot.
+//
+// Two state banks hold the per-step state (positions, velocities, angular
+// velocities, active flag); the step kernel reads bank s and writes bank s^1.
+// Two property banks hold what only moves when the storage is reordered
+// (radii, masses, stiffness, damping, pId, contact history).  The control
+// block (Ctl) in device memory says which bank is current, so captured CUDA
+// graphs stay valid whatever the device decided at earlier steps.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gdem {
+
+constexpr int kBlock = 256;
+constexpr unsigned kNoKey = 0xFFFFFFFFu;  // sort key of inactive particles (sorted last)
+constexpr int kMaxStencil = 1;            // neighbour-cell stencil radius (cell >= cutoff)
+constexpr int kBvhStack = 64;
+
+// One triangle of the wall mesh with everything dist_triangle reads
+// (cpu_dem.cu:12-205), 256 bytes so a triangle is 8 full sectors.
+struct __align__(16) TriRec {
+    double n[3], d;
+    double v0[3], v1[3], v2[3];
+    double e01[3], e02[3], e12[3];
+    double d00, d01, d11, denom, d00inv, d11inv, d22inv;
+    int i0, i1, i2, e0, e1, e2;
+};
+static_assert(sizeof(TriRec) == 256, "TriRec must be 256 bytes");
+
+// LBVH node: internal nodes [0, T-1), leaves [T-1, 2T-1).
+struct __align__(16) BNode {
+    double lo[3], hi[3];
+    int left, right;   // child node indices (internal nodes)
+    int tri;           // triangle index (leaves), -1 otherwise
+    int parent;
+};
+static_assert(sizeof(BNode) == 64, "BNode must be 64 bytes");
+
+struct Ctl {
+    int s;                    // state bank holding the current state
+    int p;                    // property bank holding current properties/history
+    unsigned refresh;         // set when some particle moved beyond the threshold
+    unsigned error;           // GDEM_EW_* bits
+    unsigned done[4];         // last-block counters (one per kernel family)
+    unsigned long long steps;
+    unsigned long long rebuilds;
+    int max_nei, max_wall;
+    int lists_valid;
+    int pad;
+};
+
+struct SBank {
+    double *x, *y, *z;
+    double *vx, *vy, *vz;
+    double *wx, *wy, *wz;
+    int* active;
+};
+
+struct PBank {
+    double *r, *rsq, *invm, *sqrtm, *invmoi, *k, *eta;
+    int* pid;
+    int* nc;                  // particle contacts in history
+    int* hid;                 // [hcap * n] pId of the contact partner
+    double *hx, *hy, *hz;     // [hcap * n] tangential spring
+    int* ncw;                 // wall contacts in history
+    int* hwid;                // [hwcap * n] triangle index
+    double *hwx, *hwy, *hwz;  // [hwcap * n]
+};
+
+struct View {
+    int n;
+    SBank S[2];
+    PBank P[2];
+    Ctl* ctl;
+    // lists (rebuilt, not reordered)
+    int *nei, *nnei, *neiw, *nneiw;
+    double *refx, *refy, *refz;
+    int nei_cap, wall_cap, hist_cap, histw_cap;
+    // per-step force/torque output
+    double *fx, *fy, *fz, *tx, *ty, *tz;
+    double* ftmp;        // [6 * n] scratch for reordering the force outputs
+    int store_forces;
+    // sort scratch (ping-pong) and cell list
+    uint32_t* keys[2];
+    int* vals[2];
+    uint32_t* rs_hist;   // [256 * rs_blocks]
+    uint32_t* rs_tot;    // [256]
+    int rs_blocks;
+    int *cell_start, *cell_end;
+    int ncells, sizex, sizey, sizez;
+    int reorder;
+    // mesh
+    const TriRec* tri;
+    const BNode* bvh;
+    int ntri;
+    int bvh_root;
+    // scalars
+    double dt, mu;
+    double gx, gy, gz;
+    double minx, miny, minz, maxx, maxy, maxz;
+    double invdx, invdy, invdz;
+    double skin, thresh_sq;
+};
+
+// ---------------------------------------------------------------- Morton
+// 10-bit spread and interleave (x -> bit 2, y -> bit 1, z -> bit 0), the
+// encoding of BoundingBox.h:125-135.
+__host__ __device__ __forceinline__ uint32_t spread10(uint32_t v) {
+    v &= 0x3ffu;
+    v = (v | (v << 16)) & 0x030000FFu;
+    v = (v | (v << 8)) & 0x0300F00Fu;
+    v = (v | (v << 4)) & 0x030C30C3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+__host__ __device__ __forceinline__ uint32_t morton3(uint32_t x, uint32_t y, uint32_t z) {
+    return (spread10(x) << 2) | (spread10(y) << 1) | spread10(z);
+}
+__host__ __device__ __forceinline__ uint32_t compact10(uint32_t v) {
+    v &= 0x09249249u;
+    v = (v | (v >> 2)) & 0x030C30C3u;
+    v = (v | (v >> 4)) & 0x0300F00Fu;
+    v = (v | (v >> 8)) & 0x030000FFu;
+    v = (v | (v >> 16)) & 0x000003FFu;
+    return v;
+}
+
+// Cell coordinate with the +1 ghost offset: floor((x - min) * invd) + 1
+// (BoundingBox.cu:787-789).
+__device__ __forceinline__ int cell_coord(double x, double mn, double invd) {
+    return (int)floor((x - mn) * invd) + 1;
+}
+
+// ---------------------------------------------------------------- closest feature
+struct Feature {
+    double nx, ny, nz, dist;
+    int hit;
+};
+
+// Sphere centre p against triangle t: the closest-feature classification of
+// dist_triangle (cpu_dem.cu:12-205) with the contact radius squared `rsq`.
+// FP64 operation order is kept term by term; compile without FMA contraction.
+__device__ __forceinline__ Feature closest_feature(double px, double py, double pz, double rsq,
+                                                   const TriRec& T) {
+    Feature res;
+    res.nx = 0.;
+    res.ny = 0.;
+    res.nz = 0.;
+    res.dist = 1.e10;
+    res.hit = -2;
+    double dist = 0.;
+    dist += T.n[0] * px;
+    dist += T.n[1] * py;
+    dist += T.n[2] * pz;
+    dist += T.d;
+    double distsq = dist * dist;
+    if (distsq > rsq) return res;
+
+    const double apx = px - T.v0[0], apy = py - T.v0[1], apz = pz - T.v0[2];
+    const double d20 = apx * T.e01[0] + apy * T.e01[1] + apz * T.e01[2];
+    const double d21 = apx * T.e02[0] + apy * T.e02[1] + apz * T.e02[2];
+    const double v = (T.d11 * d20 - T.d01 * d21) * T.denom;
+    const double w = (T.d00 * d21 - T.d01 * d20) * T.denom;
+    const double u = 1.0 - v - w;
+    if (u > 0. && v > 0. && w > 0.) {
+        const double sign = dist < 0 ? -1.0 : 1.0;
+        res.nx = sign * T.n[0];
+        res.ny = sign * T.n[1];
+        res.nz = sign * T.n[2];
+        res.dist = sign * dist;
+        res.hit = -1;
+        return res;
+    }
+    double qx, qy, qz;  // closest point of the triangle
+    int hit;
+    if (v <= 0. && w <= 0.0) {
+        qx = T.v0[0]; qy = T.v0[1]; qz = T.v0[2];
+        hit = T.i0;
+    } else if (u <= 0. && w <= 0.0) {
+        qx = T.v1[0]; qy = T.v1[1]; qz = T.v1[2];
+        hit = T.i1;
+    } else if (u <= 0. && v <= 0.0) {
+        qx = T.v2[0]; qy = T.v2[1]; qz = T.v2[2];
+        hit = T.i2;
+    } else if (u <= 0.0) {
+        const double bx = px - T.v1[0], by = py - T.v1[1], bz = pz - T.v1[2];
+        double t = (bx * T.e12[0] + by * T.e12[1] + bz * T.e12[2]) * T.d22inv;
+        t = fmax(0., fmin(1.0, t));
+        qx = T.v1[0] + t * T.e12[0];
+        qy = T.v1[1] + t * T.e12[1];
+        qz = T.v1[2] + t * T.e12[2];
+        hit = T.e1;
+    } else if (v <= 0.0) {
+        double t = d21 * T.d11inv;
+        t = fmax(0., fmin(1.0, t));
+        qx = T.v0[0] + t * T.e02[0];
+        qy = T.v0[1] + t * T.e02[1];
+        qz = T.v0[2] + t * T.e02[2];
+        hit = T.e2;
+    } else {
+        double t = d20 * T.d00inv;
+        t = fmax(0., fmin(1.0, t));
+        qx = T.v0[0] + t * T.e01[0];
+        qy = T.v0[1] + t * T.e01[1];
+        qz = T.v0[2] + t * T.e01[2];
+        hit = T.e0;
+    }
+    res.nx = px - qx;
+    res.ny = py - qy;
+    res.nz = pz - qz;
+    distsq = res.nx * res.nx + res.ny * res.ny + res.nz * res.nz;
+    if (distsq < rsq) {
+        res.dist = sqrt(distsq);
+        const double inv = 1. / res.dist;
+        res.nx = inv * res.nx;
+        res.ny = inv * res.ny;
+        res.nz = inv * res.nz;
+    }
+    res.hit = hit;
+    return res;
+}
+
+// Squared distance test of a sphere of radius R around p against an AABB,
+// sphereAABBOverlapNeighbor (BVH.cu:10-42).
+__device__ __forceinline__ bool sphere_aabb(double px, double py, double pz, double Rsq,
+                                            const double* lo, const double* hi) {
+    double dx = 0.0, dy = 0.0, dz = 0.0;
+    if (px < lo[0]) dx = lo[0] - px;
+    else if (px > hi[0]) dx = px - hi[0];
+    if (py < lo[1]) dy = lo[1] - py;
+    else if (py > hi[1]) dy = py - hi[1];
+    if (pz < lo[2]) dz = lo[2] - pz;
+    else if (pz > hi[2]) dz = pz - hi[2];
+    return (dx * dx + dy * dy + dz * dz) <= Rsq;
+}
+
+// "Last block of the grid" election without waiting: every block bumps a
+// counter after its writes; the block that sees gridDim.x-1 runs the epilogue
+// and resets the counter for the next launch.
+__device__ __forceinline__ bool last_block(unsigned* counter) {
+    __shared__ bool am_last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        unsigned prev = atomicAdd(counter, 1u);
+        am_last = (prev == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (am_last) __threadfence();
+    return am_last;
+}
+
+// ---------------------------------------------------------------- launchers
+// rebuild stages (gdem_rebuild.cu)
+void launch_rebuild(const View& v, cudaStream_t st, int n, int force);
+void launch_bvh_build(TriRec* tri, const double* aabb, BNode* nodes, const uint32_t* morton_sorted,
+                      const int* sorted_idx, int* flags, int ntri, cudaStream_t st);
+void launch_tri_precompute(TriRec* rec, double* aabb, uint32_t* morton, int* idx, const double* vx,
+                           const double* vy, const double* vz, const int* tv, const int* te,
+                           const double* raw3, int ntri, const double* gmin, const double* invrange,
+                           cudaStream_t st);
+void radix_sort_pairs(uint32_t* keys0, int* vals0, uint32_t* keys1, int* vals1, uint32_t* hist,
+                      uint32_t* tot, int n, int nblocks, int first_pass, int npasses, cudaStream_t st);
+int rs_blocks_for(int n);
+void launch_finalize_oob(const View& v, cudaStream_t st);
+// step kernels (gdem_step_fp64.cu)
+void launch_step_fp64(const View& v, cudaStream_t st, cudaGraphConditionalHandle cond, int use_cond);
+// exports and small utilities (gdem_rebuild.cu)
+void launch_dist_triangle(const TriRec* tri, const double* pos, const double* r, const int* t, int m,
+                          double* out4, int* hit, cudaStream_t st);
+
+}  // namespace gdem

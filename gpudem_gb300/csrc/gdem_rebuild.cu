@@ -1,0 +1,682 @@
+// List rebuild path of the GB300 DEM engine: Morton keys, stable LSB radix
+// sort, particle reorder, cell ranges, Verlet lists, wall LBVH and wall lists.
+//
+// Reference counterparts (gpudem): dk_morton_key / update_pList_withSort
+// (BoundingBox.cu:1007, :664), radixSortUint32 / CUB SortPairs
+// (BoundingBox.cu:33, :1235), d_swap_ps (BoundingBox.cu:928), d_update_pList
+// (BoundingBox.cu:1266), k_update_neighborlist_endsort (BoundingBox.cu:1106),
+// buildBVH (BVH.cu:741), k_update_neighborlist_wall (BVH.cu:493).
+//
+// Every kernel that decides list membership uses the reference's FP64
+// arithmetic in the same operation order; this file is compiled with
+// -fmad=false so no multiply-add is contracted.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gdem_internal.cuh"
+
+namespace gdem {
+
+// ===================================================================== radix sort
+// Stable least-significant-digit radix sort of (key, value) pairs with 8-bit
+// digits.  One pass = upsweep (per-tile digit histograms, digit-major table),
+// scan (per-digit exclusive scan over tiles), downsweep (stable scatter).  The
+// scatter ranks equal digits inside a tile with __match_any_sync, so the
+// permutation is the unique stable one — the same that radixSortUint32
+// (BoundingBox.cu:33-104) and CUB's SortPairs produce.  No kernel waits on
+// another block.
+constexpr int RS_THREADS = 256;
+constexpr int RS_ROUNDS = 8;
+constexpr int RS_TILE = RS_THREADS * RS_ROUNDS;
+
+int rs_blocks_for(int n) { return n <= 0 ? 1 : (n + RS_TILE - 1) / RS_TILE; }
+
+__global__ void __launch_bounds__(RS_THREADS) k_rs_upsweep(const uint32_t* __restrict__ keys, int n,
+                                                           int shift, uint32_t* __restrict__ hist,
+                                                           int nblocks, const Ctl* ctl, int gated) {
+    if (gated && ctl->refresh == 0u) return;
+    __shared__ uint32_t cnt[256];
+    cnt[threadIdx.x] = 0;
+    __syncthreads();
+    const int base = blockIdx.x * RS_TILE;
+#pragma unroll
+    for (int r = 0; r < RS_ROUNDS; r++) {
+        const int i = base + r * RS_THREADS + threadIdx.x;
+        if (i < n) atomicAdd(&cnt[(keys[i] >> shift) & 0xFFu], 1u);
+    }
+    __syncthreads();
+    hist[threadIdx.x * nblocks + blockIdx.x] = cnt[threadIdx.x];
+}
+
+// one block per digit: exclusive scan of that digit's tile counts
+__global__ void __launch_bounds__(1024) k_rs_scan(uint32_t* __restrict__ hist, int nblocks,
+                                                  uint32_t* __restrict__ tot, const Ctl* ctl, int gated) {
+    if (gated && ctl->refresh == 0u) return;
+    __shared__ uint32_t warp_sums[32];
+    __shared__ uint32_t carry;
+    uint32_t* row = hist + (size_t)blockIdx.x * nblocks;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < nblocks; base += blockDim.x) {
+        const int i = base + threadIdx.x;
+        const uint32_t x = i < nblocks ? row[i] : 0u;
+        uint32_t incl = x;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        if (lane == 31) warp_sums[warp] = incl;
+        __syncthreads();
+        if (warp == 0) {
+            const int nw = blockDim.x >> 5;
+            uint32_t s = lane < nw ? warp_sums[lane] : 0u;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+                if (lane >= o) s += y;
+            }
+            if (lane < nw) warp_sums[lane] = s;  // inclusive warp prefix
+        }
+        __syncthreads();
+        const uint32_t warp_excl = warp ? warp_sums[warp - 1] : 0u;
+        const uint32_t c = carry;
+        if (i < nblocks) row[i] = c + warp_excl + incl - x;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry = c + warp_excl + incl;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) tot[blockIdx.x] = carry;
+}
+
+__global__ void __launch_bounds__(RS_THREADS) k_rs_downsweep(
+    const uint32_t* __restrict__ kin, const int* __restrict__ vin, uint32_t* __restrict__ kout,
+    int* __restrict__ vout, int n, int shift, const uint32_t* __restrict__ hist,
+    const uint32_t* __restrict__ tot, int nblocks, const Ctl* ctl, int gated) {
+    if (gated && ctl->refresh == 0u) return;
+    constexpr int NW = RS_THREADS / 32;
+    __shared__ uint32_t base[256];
+    __shared__ uint32_t wcnt[NW][256];
+    __shared__ uint32_t scan_tmp[256];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    // digit base = exclusive prefix of the digit totals + this tile's offset
+    scan_tmp[t] = tot[t];
+    __syncthreads();
+    for (int o = 1; o < 256; o <<= 1) {
+        const uint32_t y = t >= o ? scan_tmp[t - o] : 0u;
+        __syncthreads();
+        scan_tmp[t] += y;
+        __syncthreads();
+    }
+    base[t] = scan_tmp[t] - tot[t] + hist[t * nblocks + blockIdx.x];
+#pragma unroll
+    for (int w = 0; w < NW; w++) wcnt[w][t] = 0;
+    __syncthreads();
+    const unsigned lt_mask = (1u << lane) - 1u;
+    const int tile = blockIdx.x * RS_TILE;
+    for (int r = 0; r < RS_ROUNDS; r++) {
+        const int i = tile + r * RS_THREADS + t;
+        const bool valid = i < n;
+        uint32_t key = 0;
+        int val = 0;
+        uint32_t d = 256u;  // invalid lanes get a digit of their own
+        if (valid) {
+            key = kin[i];
+            val = vin[i];
+            d = (key >> shift) & 0xFFu;
+        }
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        const uint32_t wrank = __popc(peers & lt_mask);
+        if (valid && (peers & lt_mask) == 0u) wcnt[warp][d] = __popc(peers);
+        __syncthreads();
+        // per digit: exclusive prefix over warps, then advance the base
+        uint32_t run = 0;
+#pragma unroll
+        for (int w = 0; w < NW; w++) {
+            const uint32_t c = wcnt[w][t];
+            wcnt[w][t] = run;
+            run += c;
+        }
+        __syncthreads();
+        if (valid) {
+            const uint32_t dst = base[d] + wcnt[warp][d] + wrank;
+            kout[dst] = key;
+            vout[dst] = val;
+        }
+        __syncthreads();
+        base[t] += run;
+#pragma unroll
+        for (int w = 0; w < NW; w++) wcnt[w][t] = 0;
+        __syncthreads();
+    }
+}
+
+static void rs_passes(uint32_t* k0, int* v0, uint32_t* k1, int* v1, uint32_t* hist, uint32_t* tot,
+                      int n, int nblocks, int first_pass, int npasses, cudaStream_t st,
+                      const Ctl* ctl, int gated) {
+    uint32_t* ks[2] = {k0, k1};
+    int* vs[2] = {v0, v1};
+    for (int p = 0; p < npasses; p++) {
+        const int shift = 8 * (first_pass + p);
+        const int a = p & 1;
+        k_rs_upsweep<<<nblocks, RS_THREADS, 0, st>>>(ks[a], n, shift, hist, nblocks, ctl, gated);
+        k_rs_scan<<<256, 1024, 0, st>>>(hist, nblocks, tot, ctl, gated);
+        k_rs_downsweep<<<nblocks, RS_THREADS, 0, st>>>(ks[a], vs[a], ks[a ^ 1], vs[a ^ 1], n, shift,
+                                                       hist, tot, nblocks, ctl, gated);
+    }
+}
+
+void radix_sort_pairs(uint32_t* keys0, int* vals0, uint32_t* keys1, int* vals1, uint32_t* hist,
+                      uint32_t* tot, int n, int nblocks, int first_pass, int npasses,
+                      cudaStream_t st) {
+    rs_passes(keys0, vals0, keys1, vals1, hist, tot, n, nblocks, first_pass, npasses, st, nullptr, 0);
+}
+
+// ===================================================================== keys
+// Morton key of every particle from its ghost-offset cell coordinates
+// (update_pList_withSort, BoundingBox.cu:680-690).  Inactive particles get an
+// all-ones key so they sort behind every cell.
+__global__ void k_keys(View v, int gated) {
+    const Ctl* ctl = v.ctl;
+    if (gated && ctl->refresh == 0u) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.n) return;
+    const SBank S = v.S[ctl->s];
+    uint32_t key = kNoKey;
+    if (S.active[i] != 0) {  // 2 = leaving the box this step: still listed (main.cu:312-316)
+        const int cx = cell_coord(S.x[i], v.minx, v.invdx);
+        const int cy = cell_coord(S.y[i], v.miny, v.invdy);
+        const int cz = cell_coord(S.z[i], v.minz, v.invdz);
+        key = morton3((uint32_t)cx, (uint32_t)cy, (uint32_t)cz);
+    }
+    v.keys[0][i] = key;
+    v.vals[0][i] = i;
+}
+
+// Deactivate particles that left the box at the last step (state 2 -> 0);
+// run before a rebuild requested between steps.
+__global__ void k_finalize_oob(View v) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.n) return;
+    int* act = v.S[v.ctl->s].active;
+    if (act[i] == 2) act[i] = 0;
+}
+
+void launch_finalize_oob(const View& v, cudaStream_t st) {
+    k_finalize_oob<<<(v.n + kBlock - 1) / kBlock, kBlock, 0, st>>>(v);
+}
+
+// ===================================================================== reorder
+// Gather every per-particle array into sorted order (d_swap_ps,
+// BoundingBox.cu:928-1005, but with compact histories: only live slots move).
+__global__ void k_reorder(View v, int gated) {
+    Ctl* ctl = v.ctl;
+    if (gated && ctl->refresh == 0u) return;
+    const int s = ctl->s, p = ctl->p;
+    const int n = v.n;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const int src = v.vals[0][i];
+        const SBank A = v.S[s], B = v.S[s ^ 1];
+        B.x[i] = A.x[src]; B.y[i] = A.y[src]; B.z[i] = A.z[src];
+        B.vx[i] = A.vx[src]; B.vy[i] = A.vy[src]; B.vz[i] = A.vz[src];
+        B.wx[i] = A.wx[src]; B.wy[i] = A.wy[src]; B.wz[i] = A.wz[src];
+        B.active[i] = A.active[src];
+        const PBank P = v.P[p], Q = v.P[p ^ 1];
+        Q.r[i] = P.r[src]; Q.rsq[i] = P.rsq[src]; Q.invm[i] = P.invm[src];
+        Q.sqrtm[i] = P.sqrtm[src]; Q.invmoi[i] = P.invmoi[src]; Q.k[i] = P.k[src];
+        Q.eta[i] = P.eta[src]; Q.pid[i] = P.pid[src];
+        const int nc = P.nc[src];
+        Q.nc[i] = nc;
+        for (int k = 0; k < nc; k++) {
+            const size_t a = (size_t)k * n + src, b = (size_t)k * n + i;
+            Q.hid[b] = P.hid[a]; Q.hx[b] = P.hx[a]; Q.hy[b] = P.hy[a]; Q.hz[b] = P.hz[a];
+        }
+        const int ncw = P.ncw[src];
+        Q.ncw[i] = ncw;
+        for (int k = 0; k < ncw; k++) {
+            const size_t a = (size_t)k * n + src, b = (size_t)k * n + i;
+            Q.hwid[b] = P.hwid[a]; Q.hwx[b] = P.hwx[a]; Q.hwy[b] = P.hwy[a]; Q.hwz[b] = P.hwz[a];
+        }
+    }
+    if (last_block(&ctl->done[1])) {
+        if (threadIdx.x == 0) {
+            ctl->done[1] = 0;
+            ctl->s = s ^ 1;
+            ctl->p = p ^ 1;
+        }
+    }
+}
+
+// Per-step force/torque outputs follow the particles they belong to.
+__global__ void k_reorder_forces(View v, double* tmp, int gated) {
+    const Ctl* ctl = v.ctl;
+    if (gated && ctl->refresh == 0u) return;
+    const int n = v.n;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int src = v.vals[0][i];
+    double* f[6] = {v.fx, v.fy, v.fz, v.tx, v.ty, v.tz};
+    for (int c = 0; c < 6; c++) tmp[(size_t)c * n + i] = f[c][src];
+}
+__global__ void k_copy_forces(View v, const double* tmp, int gated) {
+    const Ctl* ctl = v.ctl;
+    if (gated && ctl->refresh == 0u) return;
+    const int n = v.n;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double* f[6] = {v.fx, v.fy, v.fz, v.tx, v.ty, v.tz};
+    for (int c = 0; c < 6; c++) f[c][i] = tmp[(size_t)c * n + i];
+}
+
+// ===================================================================== cells
+__global__ void k_cells_clear(View v, int gated) {
+    const Ctl* ctl = v.ctl;
+    if (gated && ctl->refresh == 0u) return;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < v.ncells; c += gridDim.x * blockDim.x) {
+        v.cell_start[c] = 0;
+        v.cell_end[c] = 0;
+    }
+}
+
+// Cell ranges from the sorted keys: equal keys are one cell, found by
+// comparing neighbours in the sorted order (no atomics; replaces
+// dk_build_cellCount + ExclusiveSum + dk_build_pList, BoundingBox.cu:1266).
+__global__ void k_cell_ranges(View v, int gated) {
+    const Ctl* ctl = v.ctl;
+    if (gated && ctl->refresh == 0u) return;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = v.n;
+    if (q >= n) return;
+    const uint32_t* key = v.keys[0];
+    const uint32_t kq = key[q];
+    if (kq == kNoKey) return;
+    const int cx = (int)compact10(kq >> 2), cy = (int)compact10(kq >> 1), cz = (int)compact10(kq);
+    if (cx >= v.sizex || cy >= v.sizey || cz >= v.sizez) {
+        atomicOr(&v.ctl->error, 0x40u);
+        return;
+    }
+    const int cell = (v.sizey * cz + cy) * v.sizex + cx;
+    if (q == 0 || key[q - 1] != kq) v.cell_start[cell] = q;
+    if (q == n - 1 || key[q + 1] != kq) v.cell_end[cell] = q + 1;
+}
+
+// ===================================================================== Verlet lists
+// One thread per particle: scan the 27 cells around its cell, keep every
+// active j != i with |xi - xj|^2 < (ri + rj + skin)^2 (the test of
+// BoundingBox.cu:1136-1144), order the row by the partner's pId (the
+// reference's index space) and record the reference position.
+template <int CAP>
+__global__ void __launch_bounds__(kBlock) k_neighbors(View v, int gated) {
+    Ctl* ctl = v.ctl;
+    if (gated && ctl->refresh == 0u) return;
+    const int n = v.n;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = ctl->s, p = ctl->p;
+    const SBank S = v.S[s];
+    const PBank P = v.P[p];
+    int count = 0;
+    if (i < n) {
+        if (S.active[i] == 0) {
+            v.nnei[i] = 0;
+        } else {
+            const double xi = S.x[i], yi = S.y[i], zi = S.z[i];
+            const double ri = P.r[i];
+            const double skin = v.skin;
+            const int cx = cell_coord(xi, v.minx, v.invdx);
+            const int cy = cell_coord(yi, v.miny, v.invdy);
+            const int cz = cell_coord(zi, v.minz, v.invdz);
+            int cand_pid[CAP];
+            int cand_j[CAP];
+            bool overflow = false;
+            for (int sz = -1; sz <= 1; sz++) {
+                const int zz = cz + sz;
+                if (zz < 0 || zz >= v.sizez) continue;
+                for (int sy = -1; sy <= 1; sy++) {
+                    const int yy = cy + sy;
+                    if (yy < 0 || yy >= v.sizey) continue;
+                    for (int sx = -1; sx <= 1; sx++) {
+                        const int xx = cx + sx;
+                        if (xx < 0 || xx >= v.sizex) continue;
+                        const int cell = (v.sizey * zz + yy) * v.sizex + xx;
+                        const int b = v.cell_start[cell], e = v.cell_end[cell];
+                        for (int q = b; q < e; q++) {
+                            const int j = v.reorder ? q : v.vals[0][q];
+                            if (j == i) continue;
+                            const double dx = xi - S.x[j];
+                            const double dy = yi - S.y[j];
+                            const double dz = zi - S.z[j];
+                            const double distsq = dx * dx + dy * dy + dz * dz;
+                            const double R = ri + P.r[j] + skin;
+                            if (distsq < R * R) {
+                                const int pj = P.pid[j];
+                                if (count >= CAP) {
+                                    overflow = true;
+                                    continue;
+                                }
+                                // insertion by pId keeps the row sorted as it grows
+                                int k = count;
+                                while (k > 0 && cand_pid[k - 1] > pj) {
+                                    cand_pid[k] = cand_pid[k - 1];
+                                    cand_j[k] = cand_j[k - 1];
+                                    k--;
+                                }
+                                cand_pid[k] = pj;
+                                cand_j[k] = j;
+                                count++;
+                            }
+                        }
+                    }
+                }
+            }
+            if (overflow || count > v.nei_cap) atomicOr(&ctl->error, 0x1u);
+            const int m = count < v.nei_cap ? count : v.nei_cap;
+            for (int k = 0; k < m; k++) v.nei[(size_t)k * n + i] = cand_j[k];
+            v.nnei[i] = m;
+            v.refx[i] = xi;
+            v.refy[i] = yi;
+            v.refz[i] = zi;
+        }
+    }
+    // longest row, for capacity reporting
+    int wmax = count;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) wmax = max(wmax, __shfl_xor_sync(0xffffffffu, wmax, o));
+    if ((threadIdx.x & 31) == 0 && wmax > 0) atomicMax(&ctl->max_nei, wmax);
+}
+
+// ===================================================================== wall lists
+// LBVH traversal with an explicit stack; a triangle joins the list when its
+// AABB and its closest feature are within r + skin (BVH.cu:493-540, with
+// sphereAABBOverlapNeighbor and dist_triangle_neighbor).  The set does not
+// depend on the tree shape: an ancestor's box contains its leaves' boxes, so
+// the box test never rejects an ancestor of a leaf that passes.  Rows are
+// sorted by triangle index, as BVH.cu:538 does.
+template <int CAP>
+__global__ void __launch_bounds__(kBlock) k_wall_lists(View v, int gated) {
+    Ctl* ctl = v.ctl;
+    if (gated && ctl->refresh == 0u) return;
+    const int n = v.n;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = ctl->s, p = ctl->p;
+    int count = 0;
+    if (i < n) {
+        const SBank S = v.S[s];
+        const PBank P = v.P[p];
+        if (S.active[i] == 0 || v.ntri == 0) {
+            v.nneiw[i] = 0;
+        } else {
+            const double px = S.x[i], py = S.y[i], pz = S.z[i];
+            const double R = P.r[i] + v.skin;
+            const double Rsq = R * R;
+            int cand[CAP];
+            bool overflow = false;
+            int stack[kBvhStack];
+            int sp = 0;
+            stack[sp++] = v.bvh_root;
+            while (sp > 0) {
+                const int node = stack[--sp];
+                const BNode& B = v.bvh[node];
+                if (!sphere_aabb(px, py, pz, Rsq, B.lo, B.hi)) continue;
+                if (B.tri >= 0) {
+                    const int t = B.tri;
+                    const Feature f = closest_feature(px, py, pz, Rsq, v.tri[t]);
+                    if (f.dist < P.r[i] + v.skin) {
+                        if (count >= CAP) {
+                            overflow = true;
+                            continue;
+                        }
+                        int k = count;
+                        while (k > 0 && cand[k - 1] > t) {
+                            cand[k] = cand[k - 1];
+                            k--;
+                        }
+                        cand[k] = t;
+                        count++;
+                    }
+                } else {
+                    if (sp + 2 > kBvhStack) {
+                        atomicOr(&ctl->error, 0x10u);
+                        break;
+                    }
+                    stack[sp++] = B.left;
+                    stack[sp++] = B.right;
+                }
+            }
+            if (overflow || count > v.wall_cap) atomicOr(&ctl->error, 0x2u);
+            const int m = count < v.wall_cap ? count : v.wall_cap;
+            for (int k = 0; k < m; k++) v.neiw[(size_t)k * n + i] = cand[k];
+            v.nneiw[i] = m;
+        }
+    }
+    int wmax = count;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) wmax = max(wmax, __shfl_xor_sync(0xffffffffu, wmax, o));
+    if ((threadIdx.x & 31) == 0 && wmax > 0) atomicMax(&ctl->max_wall, wmax);
+    // the last block closes the rebuild: clear the request, count it
+    if (last_block(&ctl->done[2])) {
+        if (threadIdx.x == 0) {
+            ctl->done[2] = 0;
+            ctl->refresh = 0u;
+            ctl->rebuilds += 1ull;
+            ctl->lists_valid = 1;
+        }
+    }
+}
+
+static inline int grid_for(int n) { return (n + kBlock - 1) / kBlock; }
+
+void launch_rebuild(const View& v, cudaStream_t st, int n, int force) {
+    const int gated = force ? 0 : 1;
+    const int g = grid_for(n);
+    k_keys<<<g, kBlock, 0, st>>>(v, gated);
+    rs_passes(v.keys[0], v.vals[0], v.keys[1], v.vals[1], v.rs_hist, v.rs_tot, n, v.rs_blocks, 0, 4, st,
+              v.ctl, gated);
+    if (v.reorder) {
+        if (v.store_forces) {
+            k_reorder_forces<<<g, kBlock, 0, st>>>(v, v.ftmp, gated);
+            k_copy_forces<<<g, kBlock, 0, st>>>(v, v.ftmp, gated);
+        }
+        k_reorder<<<g, kBlock, 0, st>>>(v, gated);
+    }
+    const int gc = grid_for(v.ncells) < 4096 ? grid_for(v.ncells) : 4096;
+    k_cells_clear<<<gc, kBlock, 0, st>>>(v, gated);
+    k_cell_ranges<<<g, kBlock, 0, st>>>(v, gated);
+    if (v.nei_cap <= 32)
+        k_neighbors<32><<<g, kBlock, 0, st>>>(v, gated);
+    else if (v.nei_cap <= 64)
+        k_neighbors<64><<<g, kBlock, 0, st>>>(v, gated);
+    else
+        k_neighbors<128><<<g, kBlock, 0, st>>>(v, gated);
+    if (v.wall_cap <= 16)
+        k_wall_lists<16><<<g, kBlock, 0, st>>>(v, gated);
+    else if (v.wall_cap <= 32)
+        k_wall_lists<32><<<g, kBlock, 0, st>>>(v, gated);
+    else
+        k_wall_lists<64><<<g, kBlock, 0, st>>>(v, gated);
+}
+
+// ===================================================================== mesh
+// Per-triangle precompute of load_ascii_stl_double (TriangleMesh.cu:560-630)
+// from welded vertices (tv = sorted vertex ids, te = edge ids + nShift) and
+// the raw third corner (the plane offset uses it, TriangleMesh.cu:607), plus
+// the centroid Morton key of mortonKeyGen (TriangleMesh.cu:4-21).
+__global__ void k_tri_precompute(TriRec* rec, uint32_t* morton, int* idx, const double* vx,
+                                 const double* vy, const double* vz, const int* tv, const int* te,
+                                 const double* raw3, int ntri, double gminx, double gminy,
+                                 double gminz, double irx, double iry, double irz) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntri) return;
+    const int a = tv[3 * t + 0], b = tv[3 * t + 1], c = tv[3 * t + 2];
+    TriRec R;
+    R.v0[0] = vx[a]; R.v0[1] = vy[a]; R.v0[2] = vz[a];
+    R.v1[0] = vx[b]; R.v1[1] = vy[b]; R.v1[2] = vz[b];
+    R.v2[0] = vx[c]; R.v2[1] = vy[c]; R.v2[2] = vz[c];
+    for (int k = 0; k < 3; k++) {
+        R.e01[k] = R.v1[k] - R.v0[k];
+        R.e02[k] = R.v2[k] - R.v0[k];
+        R.e12[k] = R.v2[k] - R.v1[k];
+    }
+    const double d00 = R.e01[0] * R.e01[0] + R.e01[1] * R.e01[1] + R.e01[2] * R.e01[2];
+    const double d01 = R.e01[0] * R.e02[0] + R.e01[1] * R.e02[1] + R.e01[2] * R.e02[2];
+    const double d11 = R.e02[0] * R.e02[0] + R.e02[1] * R.e02[1] + R.e02[2] * R.e02[2];
+    const double d22 = R.e12[0] * R.e12[0] + R.e12[1] * R.e12[1] + R.e12[2] * R.e12[2];
+    R.d00 = d00;
+    R.d01 = d01;
+    R.d11 = d11;
+    R.d00inv = 1. / d00;
+    R.d11inv = 1. / d11;
+    R.d22inv = 1. / d22;
+    R.denom = 1. / (d00 * d11 - d01 * d01);
+    // n = normalize(e01 x e02)
+    double nx = R.e01[1] * R.e02[2] - R.e01[2] * R.e02[1];
+    double ny = R.e01[2] * R.e02[0] - R.e01[0] * R.e02[2];
+    double nz = R.e01[0] * R.e02[1] - R.e01[1] * R.e02[0];
+    const double inv = 1. / sqrt(nx * nx + ny * ny + nz * nz);
+    nx = inv * nx;
+    ny = inv * ny;
+    nz = inv * nz;
+    R.n[0] = nx;
+    R.n[1] = ny;
+    R.n[2] = nz;
+    const double x = raw3[3 * t + 0], y = raw3[3 * t + 1], z = raw3[3 * t + 2];
+    R.d = -nx * x - ny * y - nz * z;
+    R.i0 = a;
+    R.i1 = b;
+    R.i2 = c;
+    R.e0 = te[3 * t + 0];
+    R.e1 = te[3 * t + 1];
+    R.e2 = te[3 * t + 2];
+    rec[t] = R;
+    const double cx = (R.v0[0] + R.v1[0] + R.v2[0]) / 3.0;
+    const double cy = (R.v0[1] + R.v1[1] + R.v2[1]) / 3.0;
+    const double cz = (R.v0[2] + R.v1[2] + R.v2[2]) / 3.0;
+    const uint32_t ix = (uint32_t)((cx - gminx) * irx);
+    const uint32_t iy = (uint32_t)((cy - gminy) * iry);
+    const uint32_t iz = (uint32_t)((cz - gminz) * irz);
+    morton[t] = morton3(ix, iy, iz);
+    idx[t] = t;
+}
+
+void launch_tri_precompute(TriRec* rec, double* /*aabb*/, uint32_t* morton, int* idx,
+                           const double* vx, const double* vy, const double* vz, const int* tv,
+                           const int* te, const double* raw3, int ntri, const double* gmin,
+                           const double* invrange, cudaStream_t st) {
+    if (ntri <= 0) return;
+    k_tri_precompute<<<grid_for(ntri), kBlock, 0, st>>>(rec, morton, idx, vx, vy, vz, tv, te, raw3,
+                                                        ntri, gmin[0], gmin[1], gmin[2], invrange[0],
+                                                        invrange[1], invrange[2]);
+}
+
+// ---- Karras (2012) LBVH over the Morton-sorted triangles.  Keys that tie are
+// told apart by their sorted position, so every key is distinct.
+__device__ __forceinline__ int lbvh_delta(const uint32_t* key, int n, int i, int j) {
+    if (j < 0 || j >= n) return -1;
+    const uint32_t a = key[i], b = key[j];
+    if (a == b) return 32 + __clz((unsigned)(i ^ j));
+    return __clz(a ^ b);
+}
+
+__global__ void k_lbvh_internal(BNode* nodes, const uint32_t* key, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    const int d = (lbvh_delta(key, n, i, i + 1) - lbvh_delta(key, n, i, i - 1)) >= 0 ? 1 : -1;
+    const int dmin = lbvh_delta(key, n, i, i - d);
+    int lmax = 2;
+    while (lbvh_delta(key, n, i, i + lmax * d) > dmin) lmax <<= 1;
+    int l = 0;
+    for (int t = lmax >> 1; t >= 1; t >>= 1)
+        if (lbvh_delta(key, n, i, i + (l + t) * d) > dmin) l += t;
+    const int j = i + l * d;
+    const int dnode = lbvh_delta(key, n, i, j);
+    int s = 0;
+    int t = l;
+    do {
+        t = (t + 1) >> 1;
+        if (lbvh_delta(key, n, i, i + (s + t) * d) > dnode) s += t;
+    } while (t > 1);
+    const int gamma = i + s * d + (d < 0 ? d : 0);
+    const int lo = i < j ? i : j, hi = i < j ? j : i;
+    const int left = (lo == gamma) ? (n - 1 + gamma) : gamma;
+    const int right = (hi == gamma + 1) ? (n - 1 + gamma + 1) : gamma + 1;
+    nodes[i].left = left;
+    nodes[i].right = right;
+    nodes[i].tri = -1;
+    nodes[left].parent = i;
+    nodes[right].parent = i;
+}
+
+// Leaves take their triangle's AABB; each leaf thread then climbs, and the
+// second thread to reach a node (atomic counter, no waiting) merges the two
+// children's boxes into it.
+__global__ void k_lbvh_refit(BNode* nodes, const double* aabb, const int* sorted_idx, int* flags, int n) {
+    const int l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= n) return;
+    const int leaf = n - 1 + l;
+    const int t = sorted_idx[l];
+    BNode& L = nodes[leaf];
+    for (int k = 0; k < 3; k++) {
+        L.lo[k] = aabb[6 * t + k];
+        L.hi[k] = aabb[6 * t + 3 + k];
+    }
+    L.tri = t;
+    L.left = L.right = -1;
+    if (n == 1) return;
+    __threadfence();
+    int node = L.parent;
+    while (node >= 0) {
+        const int prev = atomicAdd(&flags[node], 1);
+        if (prev == 0) return;  // first child to arrive stops here
+        __threadfence();
+        BNode& N = nodes[node];
+        const BNode& A = nodes[N.left];
+        const BNode& B = nodes[N.right];
+        for (int k = 0; k < 3; k++) {
+            const double alo = __ldcg(&A.lo[k]), blo = __ldcg(&B.lo[k]);
+            const double ahi = __ldcg(&A.hi[k]), bhi = __ldcg(&B.hi[k]);
+            N.lo[k] = alo < blo ? alo : blo;
+            N.hi[k] = ahi > bhi ? ahi : bhi;
+        }
+        __threadfence();
+        node = N.parent;
+    }
+}
+
+__global__ void k_lbvh_init(BNode* nodes, int* flags, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < 2 * n - 1) nodes[i].parent = -1;
+    if (i < n) flags[i] = 0;
+}
+
+void launch_bvh_build(TriRec* /*tri*/, const double* aabb, BNode* nodes,
+                      const uint32_t* morton_sorted, const int* sorted_idx, int* flags, int ntri,
+                      cudaStream_t st) {
+    if (ntri <= 0) return;
+    k_lbvh_init<<<grid_for(2 * ntri), kBlock, 0, st>>>(nodes, flags, ntri);
+    if (ntri > 1) k_lbvh_internal<<<grid_for(ntri - 1), kBlock, 0, st>>>(nodes, morton_sorted, ntri);
+    k_lbvh_refit<<<grid_for(ntri), kBlock, 0, st>>>(nodes, aabb, sorted_idx, flags, ntri);
+}
+
+// ===================================================================== probes
+__global__ void k_dist_triangle(const TriRec* tri, const double* pos, const double* r, const int* t,
+                                int m, double* out4, int* hit) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= m) return;
+    const double rr = r[q];
+    const double rsq = rr * rr;
+    const Feature f = closest_feature(pos[3 * q], pos[3 * q + 1], pos[3 * q + 2], rsq, tri[t[q]]);
+    out4[4 * q + 0] = f.nx;
+    out4[4 * q + 1] = f.ny;
+    out4[4 * q + 2] = f.nz;
+    out4[4 * q + 3] = f.dist;
+    hit[q] = f.dist < 1e9 ? f.hit : -2;
+}
+
+void launch_dist_triangle(const TriRec* tri, const double* pos, const double* r, const int* t, int m,
+                          double* out4, int* hit, cudaStream_t st) {
+    if (m <= 0) return;
+    k_dist_triangle<<<grid_for(m), kBlock, 0, st>>>(tri, pos, r, t, m, out4, hit);
+}
+
+}  // namespace gdem

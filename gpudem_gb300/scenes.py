@@ -293,25 +293,38 @@ def lognormal_radii(n, rng, median=1e-3, sigma=0.15, lo=0.6e-3, hi=1.6e-3):
     return np.clip(r, lo, hi)
 
 
-def config3_helical_chute(n=1_000_000, seed=3, n_tri=50_000) -> Scene:
+def config3_helical_chute(n=1_000_000, seed=3, n_tri=50_000, radius=0.3, pitch=0.1, width=0.12,
+                          v_sigma=0.0) -> Scene:
     """1e6 lognormal spheres (median 1 mm, sigma_log 0.15, clipped [0.6,1.6] mm)
-    above a seeded helical chute (radius 0.3 m, pitch 0.1 m, ~5e4 triangles),
-    released from a lattice in an annular-sector inlet over the ramp.  HM
-    material E=5e6, nu=0.3, e=0.5, mu=0.5; dt=1e-6 s."""
+    over a seeded helical chute (radius 0.3 m, pitch 0.1 m, 2 turns, ~5e4
+    triangles).  The spheres start on a jittered lattice filling the annulus
+    above the ramp (radii [radius-width, radius]) from just above the ramp's
+    highest point upwards, in a seeded random order of lattice sites.  HM
+    material E=5e6 Pa, nu=0.3, e=0.5, mu=0.5; dt=1e-6 s.  `v_sigma` adds
+    seeded Gaussian initial velocities (m/s)."""
     rng = np.random.default_rng(seed)
     radii = lognormal_radii(n, rng)
-    tris = helical_chute_mesh(n_target=n_tri, seed=seed)
-    # inlet: a box over the start of the ramp, filled as a lattice
+    tris = helical_chute_mesh(radius=radius, pitch=pitch, width=width, n_target=n_tri, seed=seed)
     rmax = float(radii.max())
     a = 2.0 * rmax * 1.05
-    nx = 40
-    nz = 40
-    ny = int(math.ceil(n / (nx * nz)))
-    lo = np.array([0.3 - 0.12 + 0.004, 0.01, -0.5 * nz * a])
-    hi = lo + np.array([nx * a + 2 * rmax + 1e-9, ny * a + 2 * rmax + 1e-9, nz * a + 2 * rmax + 1e-9])
-    x = lattice_packing(n, radii, lo, hi, rng, gap=0.05)
+    r_in, r_out = radius - width + rmax + 1e-3, radius - rmax - 1e-3
+    xs = np.arange(-r_out, r_out + 1e-12, a)
+    X, Z = np.meshgrid(xs, xs, indexing="ij")
+    rr = np.hypot(X, Z)
+    keep = (rr >= r_in) & (rr <= r_out)
+    cols = np.stack([X[keep], Z[keep]], 1)
+    layers = int(math.ceil(n / cols.shape[0]))
+    y0 = 0.01 + rmax
+    sites = rng.permutation(cols.shape[0] * layers)[:n]
+    col = sites % cols.shape[0]
+    lay = sites // cols.shape[0]
+    x = np.stack([cols[col, 0], y0 + lay * a, cols[col, 1]], 1)
+    x += (rng.random((n, 3)) - 0.5) * (0.05 * rmax)
+    lo = x.min(0) - rmax
+    hi = x.max(0) + rmax
     m = sphere_mass(2500.0, radii)
     k = np.full(n, stiffness_from_E(5e6, 1e-3))
+    v = rng.normal(0.0, v_sigma, (n, 3)) if v_sigma > 0 else None
     return Scene(x=x, r=radii, m=m, k=k, eta=eta_const(k, 0.5), mu=0.5, dt=1e-6,
-                 tris=tris, inlet_lo=lo, inlet_hi=hi, E=5e6, nu=0.3, e=0.5,
+                 tris=tris, inlet_lo=lo, inlet_hi=hi, v=v, E=5e6, nu=0.3, e=0.5,
                  name=f"helical-chute-{n}")

@@ -1,0 +1,217 @@
+/*
+ * gdem.h — C ABI of the GB300 DEM step engine (libgdem.so).
+ *
+ * The engine replaces gpudem's per-timestep device path
+ *   void device_dem_verlet_verlet(ParticleSys<DeviceMemory>*, BoundingBox*,
+ *                                 TriangleMesh*, BVH*, int gridSize, int blockSize)
+ * (reference device_dem.h:112, device_dem.cu:1195) and the list builders it
+ * calls.  Everything here is plain C: opaque handle, plain pointers and sizes,
+ * int status codes, no exceptions across the boundary.  Host arrays use the
+ * reference's layouts (ParticleSystem.h member list: xyz-interleaved vectors,
+ * MAX_NEI-strided history rows), indexed by particle id (pId) — the index space
+ * of the reference CPU path, which never reorders particles.
+ *
+ * Threading: calls on one handle are not thread-safe.  Work is enqueued on the
+ * handle's own CUDA stream; gdem_step returns without waiting.  Every call that
+ * returns data to the host waits for the stream first.
+ */
+#ifndef GDEM_H
+#define GDEM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (return value of every call) ---- */
+#define GDEM_OK 0
+#define GDEM_ERR_ARG 1        /* invalid argument or size */
+#define GDEM_ERR_CUDA 2       /* a CUDA runtime call failed (see gdem_last_error) */
+#define GDEM_ERR_CAPACITY 3   /* a list or history capacity overflowed on the device */
+#define GDEM_ERR_STATE 4      /* call out of order (e.g. step before import) */
+#define GDEM_ERR_RANGE 5      /* domain too large for 10-bit Morton cell coordinates */
+#define GDEM_ERR_DEVICE 6     /* device error word set (see gdem_stats.error_word) */
+
+/* ---- device error word bits (gdem_stats.error_word) ---- */
+#define GDEM_EW_NEI_OVERFLOW 0x1u    /* Verlet list longer than nei_capacity */
+#define GDEM_EW_WALL_OVERFLOW 0x2u   /* wall list longer than wall_capacity */
+#define GDEM_EW_HIST_OVERFLOW 0x4u   /* more particle contacts than hist_capacity */
+#define GDEM_EW_HISTW_OVERFLOW 0x8u  /* more wall contacts than hist_wall_capacity */
+#define GDEM_EW_BVH_STACK 0x10u      /* BVH traversal stack exhausted */
+#define GDEM_EW_NONFINITE 0x20u      /* NaN or Inf in a position or velocity */
+#define GDEM_EW_CELL_RANGE 0x40u     /* active particle outside the cell grid */
+
+/* ---- modes ---- */
+#define GDEM_FP64 0           /* plain FP64, bit-compatible with the reference CPU path */
+#define GDEM_MIXED 1          /* FP64 positions/integration, FP32 contact math, Kahan history */
+#define GDEM_LINEAR 0         /* linear spring-dashpot + Coulomb (cpu_dem.cu:953, :783) */
+#define GDEM_HERTZ_MINDLIN 1  /* Hertz normal + Mindlin tangential + Coulomb (+ rolling) */
+
+typedef struct gdem_handle gdem_handle;
+
+/* Engine creation parameters.  Zero / negative values select the default
+ * noted on each field. */
+typedef struct gdem_desc {
+    int n_particles;        /* particles in the scene (> 0) */
+    int precision;          /* GDEM_FP64 (default) or GDEM_MIXED */
+    int model;              /* GDEM_LINEAR (default) or GDEM_HERTZ_MINDLIN */
+    int nei_capacity;       /* Verlet neighbours per particle, default 64 (reference MAX_NEI=100) */
+    int wall_capacity;      /* wall-list triangles per particle, default 32 */
+    int hist_capacity;      /* particle contacts kept in history, default 32 */
+    int hist_wall_capacity; /* wall contacts kept in history, default 16 */
+    int reorder;            /* 1: Morton-reorder particle storage at each list rebuild (default), 0: no */
+    int store_forces;       /* 1: keep the last step's force and torque per particle */
+    int steps_per_graph;    /* steps unrolled per CUDA graph launch, default 8 */
+    double dt;              /* time step (ParticleSysShared::dt) */
+    double mu;              /* Coulomb friction coefficient (ParticleSysShared::mu) */
+    double g[3];            /* gravity (ParticleSysShared::g) */
+    double box_min[3];      /* BoundingBox min/max (BoundingBox.cu:448-478) */
+    double box_max[3];
+    double cell_size;       /* <= 0: 4 * r_max (BoundingBox.cu:381) */
+    double skin;            /* <= 0: r_max (BoundingBox.cu:386) */
+    double refresh_thresh;  /* <= 0: skin / 2 (BoundingBox.cu:387) */
+    /* Hertz-Mindlin material (model == GDEM_HERTZ_MINDLIN) */
+    double youngs_modulus;
+    double poisson_ratio;
+    double restitution;
+    double rolling_friction;
+} gdem_desc;
+
+/* Particle arrays in the reference layout (memberList/ParticleSystemMember_common.def).
+ * Row i is the particle with pId i.  Pointers that may be NULL say so. */
+typedef struct gdem_particles {
+    int n;
+    double* x;          /* [3n] positions */
+    double* v;          /* [3n] velocities (NULL: zero on import) */
+    double* angv;       /* [3n] angular velocities (NULL: zero on import) */
+    double* r;          /* [n] radii */
+    double* m;          /* [n] masses */
+    double* k;          /* [n] normal/tangential stiffness (linear model) */
+    double* etaconst;   /* [n] damping constant (ParticleSystem.cu:301) */
+    int* isActive;      /* [n] 1 active, 0 out of bounds (NULL: all active on import) */
+    /* contact history (NULL: empty on import; skipped on export) */
+    int hist_stride;    /* row stride of the history arrays (reference: MAX_NEI = 100) */
+    int* numCont;       /* [n] */
+    int* indHis;        /* [n*hist_stride] pIds of contacting particles, encounter order */
+    double* deltHisx;   /* [n*hist_stride] tangential spring history */
+    double* deltHisy;
+    double* deltHisz;
+    int* numContWall;   /* [n] */
+    int* indHisWall;    /* [n*hist_stride] triangle indices */
+    double* deltHisxWall;
+    double* deltHisyWall;
+    double* deltHiszWall;
+    /* export only (store_forces = 1): last step's force and torque, [3n] */
+    double* f;
+    double* mom;
+} gdem_particles;
+
+/* Reductions over the active particles (the parity observables). */
+typedef struct gdem_stats {
+    long long steps;            /* steps taken since import */
+    long long rebuilds;         /* Verlet/wall list rebuilds since import */
+    long long n_active;
+    long long n_nei;            /* sum of Verlet list lengths */
+    long long n_wall;           /* sum of wall list lengths */
+    long long n_contacts;       /* particle-particle contact history entries (each pair counted twice) */
+    long long n_wall_contacts;  /* wall contact history entries */
+    double kinetic_energy;      /* sum 0.5 m v.v + 0.5 I w.w */
+    double coordination;        /* n_contacts / n_active */
+    double packing_fraction;    /* sum of sphere volumes / volume of the particles' bounding box */
+    double max_overlap;         /* max over contacts of overlap / (2 r_i) */
+    unsigned int error_word;    /* GDEM_EW_* bits */
+    int max_nei, max_wall;      /* longest lists seen at the last rebuild */
+} gdem_stats;
+
+/* ---- lifecycle ---- */
+int gdem_create(const gdem_desc* desc, gdem_handle** out);
+int gdem_destroy(gdem_handle* h);
+const char* gdem_last_error(gdem_handle* h);   /* message of the last failing call ("" if none) */
+
+/* Wall mesh from triangle corners in file order (9 doubles per triangle), as an
+ * ASCII STL lists them.  file_tri_counts[nfiles] splits the triangles into
+ * files; vertices are welded within each file only (TriangleMesh.cu:483-533).
+ * NULL/0 means one file.  Replaces load_ascii_stl_double's welding, edge
+ * numbering and per-triangle precompute (TriangleMesh.cu:363-752) and the
+ * host BVH (BVH.cu:741), which becomes a device LBVH. */
+int gdem_set_mesh(gdem_handle* h, const double* tris, int n_tri, const int* file_tri_counts,
+                  int nfiles);
+
+/* Upload particles (replaces copyToDevice, ParticleSystem.cu:82).  Builds the
+ * Verlet and wall lists from the imported state (main.cu:152,199 do this on the
+ * host in the reference). */
+int gdem_import_particles(gdem_handle* h, const gdem_particles* p);
+
+/* Advance nsteps timesteps (device_dem_verlet_verlet, device_dem.cu:1195, once
+ * per step): contacts, integration, out-of-bounds, refresh test and, when a
+ * particle moved more than refresh_thresh, the list rebuild — decided on the
+ * device, no host synchronisation.  Asynchronous. */
+int gdem_step(gdem_handle* h, int nsteps);
+int gdem_synchronize(gdem_handle* h);   /* wait; GDEM_ERR_DEVICE if the error word is set */
+
+/* Download in pId order (replaces copyFromDevice, ParticleSystem.cu:97).
+ * Fields left NULL are skipped. */
+int gdem_export_particles(gdem_handle* h, gdem_particles* p);
+int gdem_stats_get(gdem_handle* h, gdem_stats* s);
+
+/* ---- the hot-path stages, callable one at a time ---- */
+
+/* Rebuild Morton order, cell list, Verlet lists and wall lists from the
+ * current state now (update_neighborlist + update_neighborlist_wall,
+ * BoundingBox.cu:526, BVH.cu:576). */
+int gdem_rebuild(gdem_handle* h);
+
+/* Verlet and wall lists in pId space: row p holds the pIds (resp. triangle
+ * indices) of the neighbours of particle p in ascending order, like the
+ * reference's neiList / neiListWall rows (BoundingBox.cu:579, BVH.cu:622). */
+int gdem_export_lists(gdem_handle* h, int stride, int* numNei, int* neiList, int* numNeiWall,
+                      int* neiListWall);
+
+/* Morton keys of the particles in pId order, computed as dk_morton_key /
+ * update_pList_withSort do (BoundingBox.cu:1007, :680-690). */
+int gdem_morton_keys(gdem_handle* h, uint32_t* keys);
+
+/* Cell list of the last rebuild in the layout update_pList_withSort leaves
+ * (BoundingBox.cu:664-731): sorted keys, order (pId at each sorted position),
+ * pNum/pStart over all cells, pList (sorted positions grouped by cell id).
+ * n_cells receives the cell count (BoundingBox::N); pass NULL arrays to query. */
+int gdem_export_cells(gdem_handle* h, uint32_t* keys_sorted, int* order, int* pNum, int* pStart,
+                      int* pList, int* n_cells);
+
+/* Stable LSB radix sort of n 32-bit keys with index payload 0..n-1 on the
+ * device (radixSortUint32, BoundingBox.cu:33; CUB SortPairs, :1235). */
+int gdem_sort_keys(const uint32_t* keys, int n, uint32_t* keys_sorted, int* perm);
+
+/* Closest-feature test of m (sphere, triangle) pairs on the device
+ * (dist_triangle, cpu_dem.cu:12 / device_dem.cu:12).  out4[4m] = n.xyz, dist;
+ * hitAt[m] = -1 face, vertex id, or edge id + nShift; -2 when no contact. */
+int gdem_dist_triangle(gdem_handle* h, const double* pos, const double* r, const int* tri, int m,
+                       double* out4, int* hitAt);
+
+/* Per-triangle precompute of the current mesh (TriangleMesh.cu:560-667):
+ * rec[29*n_tri] doubles per triangle in the order
+ *   n.xyz, d, v0.xyz, v1.xyz, v2.xyz, e01.xyz, e02.xyz, e12.xyz,
+ *   d00, d01, d11, denom, d00inv, d11inv, d22inv
+ * irec[6*n_tri] = tri_i0..2, tri_e0..2; aabb[6*n_tri] = minx,miny,minz,maxx,maxy,maxz;
+ * morton[n_tri] sorted centroid keys; sorted_index[n_tri] their permutation. */
+int gdem_export_mesh(gdem_handle* h, double* rec, int* irec, double* aabb, uint32_t* morton,
+                     int* sorted_index);
+
+/* ---- measurement ---- */
+
+/* The CUDA stream (cudaStream_t) every call of this handle enqueues on, for
+ * recording timing events around gdem_step. */
+int gdem_get_stream(gdem_handle* h, void** stream);
+
+/* Time the step kernel alone: `iters` launches, each bracketed by CUDA events
+ * on the handle's stream and followed by the (device-gated) list rebuild, so
+ * the state stays valid.  avg_ms receives the mean step-kernel duration.
+ * Advances the simulation by `iters` steps. */
+int gdem_profile_step(gdem_handle* h, int iters, float* avg_ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GDEM_H */
