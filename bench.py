@@ -110,107 +110,142 @@ def dist_init():
     return None, 0, 1
 
 
+def _time_steps(E, steps, warmup, stream, clk=None):
+    import torch
+    E.step(warmup)
+    E.sync()
+    st0 = E.stats()
+    start = torch.cuda.Event(enable_timing=True)
+    stop = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    if clk is not None:
+        clk.__enter__()
+    start.record(stream)
+    E.step(steps)
+    stop.record(stream)
+    stop.synchronize()
+    torch.cuda.synchronize()
+    if clk is not None:
+        clk.__exit__()
+    st1 = E.stats()
+    return start.elapsed_time(stop), st0, st1
+
+
 def run_engine(args):
     import torch
     from gpudem_gb300 import engine, scenes
     dist, rank, ws = dist_init()
     lrank = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(lrank)
-    os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(lrank))
     sc = scenes.config3_helical_chute(n=args.n, n_tri=args.ntri, v_sigma=args.v_sigma)
+    kw = dict(model=args.model, reorder=True, nei_capacity=args.nei_cap, steps_per_graph=8,
+              skin=args.skin if args.skin > 0 else None)
     t0 = time.time()
-    E = engine.Engine(sc, precision=args.precision, reorder=True, nei_capacity=args.nei_cap,
-                      steps_per_graph=8, skin=args.skin if args.skin > 0 else None)
+    E = engine.Engine(sc, precision=args.precision, **kw)
     setup_s = time.time() - t0
     stream = torch.cuda.ExternalStream(E.stream())
-    E.step(args.warmup)
-    E.sync()
-    st0 = E.stats()
-    start = torch.cuda.Event(enable_timing=True)
-    stop = torch.cuda.Event(enable_timing=True)
     if dist:
         dist.barrier()
-    clk = Clocks(os.path.join(ROOT, "gpurun_out", f"clocks_r{rank}.csv") if os.path.isdir(
-        os.path.join(ROOT, "gpurun_out")) else f"/tmp/gdem_clocks_{os.getpid()}.csv")
-    with clk:
-        torch.cuda.synchronize()
-        start.record(stream)
-        E.step(args.steps)
-        stop.record(stream)
-        stop.synchronize()
-        torch.cuda.synchronize()
-    ms = start.elapsed_time(stop)
+    out_dir = os.path.join(ROOT, "gpurun_out") if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp"
+    clk = Clocks(os.path.join(out_dir, f"clocks_r{rank}.csv"))
+    ms, st0, st1 = _time_steps(E, args.steps, args.warmup, stream, clk)
     if dist:
         t = torch.tensor([ms], dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
-    st1 = E.stats()
     n_act = 0.5 * (st0["n_active"] + st1["n_active"])
     value = n_act * args.steps * ws / (ms / 1e3)
-    # force-kernel roofline: step kernel alone, CUDA events on the engine stream
+    # dominant kernel: the step kernel alone, CUDA events on the engine stream
     k_ms = E.profile_step(args.profile_iters)
     stk = E.stats()
-    bytes_launch = algorithmic_bytes(stk, stk["n_active"])
+    mixed = args.precision == "mixed"
+    bytes_launch = algorithmic_bytes(stk, stk["n_active"], s=4 if mixed else 8, s_h=8)
     peak, peak_kind = _peaks()
     achieved = bytes_launch / (k_ms / 1e3) / 1e9
+    reb = int(st1["rebuilds"] - st0["rebuilds"])
+    E.close()
+    extra = {}
+    if mixed and not args.no_fp64:
+        # the same engine in plain FP64 on the same workload (the ratio's denominator)
+        F = engine.Engine(sc, precision="fp64", **kw)
+        fstream = torch.cuda.ExternalStream(F.stream())
+        fsteps = max(10, args.steps // 4)
+        fms, f0, f1 = _time_steps(F, fsteps, args.warmup, fstream)
+        fval = 0.5 * (f0["n_active"] + f1["n_active"]) * fsteps / (fms / 1e3)
+        F.close()
+        extra = {"fp64_value": fval, "fp64_steps": fsteps, "mixed_over_fp64": value / fval}
+        if args.error_steps > 0:
+            extra.update(position_error(sc, kw, args.error_steps))
     # end to end through the C ABI with host buffers
-    e2e = run_e2e(args, sc)
+    e2e = run_e2e(args, sc, kw) if not args.no_e2e else None
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+        "dtype": "f32+f64" if mixed else "f64",
         "data": "synthetic (seeded lognormal spheres on a lattice over a generated helical chute)",
-        "config": {"workload": f"helical chute, {args.n} lognormal spheres, {sc.tris.shape[0]} triangles, "
-                               f"dt=1e-6 s, linear spring-dashpot, {args.precision}",
+        "config": {"workload": f"helical chute, {args.n} lognormal spheres (median 1 mm, sigma_log 0.15), "
+                               f"{sc.tris.shape[0]} triangles, dt=1e-6 s, {args.model}, {args.precision}",
                    "n_particles": args.n, "n_triangles": int(sc.tris.shape[0]), "precision": args.precision,
-                   "model": "linear", "l2": "inputs larger than L2 (state + lists > 129 MB per step)",
+                   "model": args.model, "l2": "inputs larger than L2 (state + lists > 129 MB per step)",
                    "parallelism": "replicas" if ws > 1 else "single GPU",
-                   "rebuilds_in_timed_region": int(st1["rebuilds"] - st0["rebuilds"]),
-                   "setup_s": round(setup_s, 2)},
+                   "rebuilds_in_timed_region": reb, "setup_s": round(setup_s, 2), **extra},
         "clocks": clk.summary(),
-        "gpu_launches": None,
+        # one step kernel per step + the rebuild kernels of each rebuild
+        # (keys, 4 x 3 sort passes, reorder, cell clear, cell ranges, Verlet, walls)
+        "gpu_launches": args.steps + reb * 18,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None, "peak_kind": f"{peak_kind} hbm_gbs",
-                     "kernel": "k_step_fp64", "kernel_ms": k_ms, "algorithmic_bytes": bytes_launch,
+                     "frac": achieved / peak, "traffic": args.traffic,
+                     "peak_kind": f"{peak_kind} hbm_gbs",
+                     "kernel": f"k_step<{'Mixed' if mixed else 'FP64'},{args.model}>", "kernel_ms": k_ms,
+                     "algorithmic_bytes": bytes_launch,
                      "counts": {k: stk[k] for k in ("n_active", "n_nei", "n_wall", "n_contacts",
                                                     "n_wall_contacts")}},
         "e2e": e2e,
         "cpu_baseline": cpu_baseline(args, sc) if (rank == 0 and ws == 1 and not args.no_cpu) else None,
     }
-    # launches inside the timed region: one step kernel per step plus the
-    # rebuild kernels of each rebuild (19 kernels: keys, 4x3 sort, reorder,
-    # clear, ranges, neighbours, walls)
-    reb = out["config"]["rebuilds_in_timed_region"]
-    out["gpu_launches"] = args.steps + reb * 18
-    E.close()
     if rank == 0:
         print(json.dumps(out))
 
 
-def run_e2e(args, sc):
-    """Same metric through the C ABI with host buffers: import from pinned host
-    memory, K steps, positions read back every step."""
+def position_error(sc, kw, steps):
+    """max |x_mixed - x_fp64| after `steps` steps from the same state."""
+    from gpudem_gb300 import engine
+    A = engine.Engine(sc, precision="fp64", **kw)
+    A.step(steps)
+    xa = A.export_positions()
+    A.close()
+    B = engine.Engine(sc, precision="mixed", **kw)
+    B.step(steps)
+    xb = B.export_positions()
+    B.close()
+    err = float(np.max(np.abs(xa - xb)))
+    rmin = float(np.min(sc.r))
+    return {"pos_err_steps": steps, "pos_err_m": err, "pos_err_over_rmin": err / rmin}
+
+
+def run_e2e(args, sc, kw):
+    """Same metric through the C ABI with host buffers: the state uploaded from
+    host memory, K steps, positions read back into pinned host memory every
+    step (write_frame_bin's frame), all inside the timed region."""
     import torch
     from gpudem_gb300 import engine
     n = sc.n
     steps = max(1, min(args.steps, args.e2e_steps))
-    E = engine.Engine(sc, precision=args.precision, reorder=True, nei_capacity=args.nei_cap,
-                      skin=args.skin if args.skin > 0 else None)
+    E = engine.Engine(sc, precision=args.precision, **kw)
+    frame = torch.empty(3 * n, dtype=torch.float64).pin_memory().numpy()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     E.import_particles(sc)
-    h2d = n * (3 * 8 * 3 + 4 * 8)
-    d2h = 0
     for _ in range(steps):
         E.step(1)
-        x = E.export(history=False, forces=False)["x"]
-        d2h += x.nbytes
+        E.export_positions(out=frame)
     E.sync()
     dt_s = time.perf_counter() - t0
     E.close()
+    h2d = n * (4 * 8 * 3 + 4 * 8)
     return {"value": n * steps / dt_s, "unit": UNIT, "h2d_bytes_per_step": h2d / steps,
-            "d2h_bytes_per_step": d2h / steps, "steps": steps}
+            "d2h_bytes_per_step": frame.nbytes, "steps": steps}
 
 
 def cpu_baseline(args, sc):
@@ -250,12 +285,18 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=40)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--n", type=int, default=1_000_000)
     ap.add_argument("--ntri", type=int, default=50_000)
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--model", default="hertz_mindlin", choices=["linear", "hertz_mindlin"])
+    ap.add_argument("--error-steps", type=int, default=1000)
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--traffic", type=float, default=None,
+                    help="DRAM bytes per step-kernel launch from an ncu capture, if known")
     ap.add_argument("--nei-cap", type=int, default=64)
     ap.add_argument("--skin", type=float, default=-1.0)
     ap.add_argument("--v-sigma", type=float, default=0.5)

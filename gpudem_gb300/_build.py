@@ -30,6 +30,7 @@ UNITS = {
     "gdem_api.cu": True,
     "gdem_rebuild.cu": True,
     "gdem_step_fp64.cu": True,
+    "gdem_step_mixed.cu": False,
     "gdem_stats.cu": True,
 }
 

@@ -21,6 +21,7 @@ EXPORTED = [
     "gdem_step", "gdem_synchronize", "gdem_export_particles", "gdem_stats_get", "gdem_rebuild",
     "gdem_export_lists", "gdem_morton_keys", "gdem_export_cells", "gdem_sort_keys",
     "gdem_dist_triangle", "gdem_export_mesh", "gdem_get_stream", "gdem_profile_step",
+    "gdem_export_positions",
 ]
 
 
@@ -105,6 +106,7 @@ def load(build_if_missing: bool = False):
     L.gdem_dist_triangle.argtypes = [vp, vp, vp, vp, C.c_int, vp, vp]
     L.gdem_export_mesh.argtypes = [vp, vp, vp, vp, vp, vp]
     L.gdem_get_stream.argtypes = [vp, C.POINTER(vp)]
+    L.gdem_export_positions.argtypes = [vp, vp]
     L.gdem_profile_step.argtypes = [vp, C.c_int, C.POINTER(C.c_float)]
     for nm in EXPORTED:
         if nm != "gdem_last_error":

@@ -1,18 +1,20 @@
 // Internal device-side layout of the GB300 DEM engine.
 //
-// Particle storage is structure-of-arrays with one array per scalar component
-// (x, y, z separately), so a warp of consecutive particles loads 256
-// contiguous bytes per component.  Per-particle rows of variable length
-// (Verlet list, wall list, contact history) are stored "slot-major"
-// (element k of particle i at [k * n + i]): consecutive threads touch
-// consecutive addresses for the same slot.
+// Per-particle data that neighbours gather lives in 16/32-byte records, so a
+// neighbour costs three vector loads:
+//   pos[i] = {x, y, z, r}           double4_32a (positions stay FP64 in every mode)
+//   vel[i] = {vx, vy, vz, 1/m}      V4 (double4_32a in FP64 mode, float4 in mixed mode)
+//   rot[i] = {wx, wy, wz, status}   V4; status 1 active, 0 inactive, 2 leaving the
+//                                   box this step (still in this step's rebuild)
+// Rows of variable length (Verlet list, wall list, contact history) are stored
+// slot-major (element k of particle i at [k * n + i]) so a warp reads one slot
+// of 32 consecutive particles in one transaction.
 //
-// Two state banks hold the per-step state (positions, velocities, angular
-// velocities, active flag); the step kernel reads bank s and writes bank s^1.
-// Two property banks hold what only moves when the storage is reordered
-// (radii, masses, stiffness, damping, pId, contact history).  The control
-// block (Ctl) in device memory says which bank is current, so captured CUDA
-// graphs stay valid whatever the device decided at earlier steps.
+// Two state banks hold pos/vel/rot; the step kernel reads bank s and writes
+// bank s^1.  Two property banks hold what moves only when the storage is
+// Morton-reordered (material record, pId, contact history).  The control block
+// (Ctl) in device memory says which bank is current, so captured CUDA graphs
+// stay valid whatever the device decided at earlier steps.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -22,8 +24,19 @@ namespace gdem {
 
 constexpr int kBlock = 256;
 constexpr unsigned kNoKey = 0xFFFFFFFFu;  // sort key of inactive particles (sorted last)
-constexpr int kMaxStencil = 1;            // neighbour-cell stencil radius (cell >= cutoff)
 constexpr int kBvhStack = 64;
+
+// ---------------------------------------------------------------- precision traits
+struct FP64 {
+    using real = double;
+    using v4 = double4_32a;
+    static constexpr bool mixed = false;
+};
+struct Mixed {
+    using real = float;
+    using v4 = float4;
+    static constexpr bool mixed = true;   // FP32 contact math, compensated spring history
+};
 
 // One triangle of the wall mesh with everything dist_triangle reads
 // (cpu_dem.cu:12-205), 256 bytes so a triangle is 8 full sectors.
@@ -58,42 +71,63 @@ struct Ctl {
     int pad;
 };
 
+template <class T>
 struct SBank {
-    double *x, *y, *z;
-    double *vx, *vy, *vz;
-    double *wx, *wy, *wz;
-    int* active;
+    double4_32a* pos;
+    typename T::v4* vel;
+    typename T::v4* rot;
 };
 
+// material record: linear model {k, etaconst, sqrt(m), 1/I};
+// Hertz-Mindlin {0, 0, sqrt(m), 1/I}
+template <class T>
 struct PBank {
-    double *r, *rsq, *invm, *sqrtm, *invmoi, *k, *eta;
+    typename T::v4* mat;
     int* pid;
-    int* nc;                  // particle contacts in history
-    int* hid;                 // [hcap * n] pId of the contact partner
-    double *hx, *hy, *hz;     // [hcap * n] tangential spring
-    int* ncw;                 // wall contacts in history
-    int* hwid;                // [hwcap * n] triangle index
-    double *hwx, *hwy, *hwz;  // [hwcap * n]
+    int* nc;                         // particle contacts in history
+    int* hid;                        // [hcap * n] pId of the contact partner
+    typename T::real *hx, *hy, *hz;  // [hcap * n] tangential spring
+    typename T::real *cx, *cy, *cz;  // [hcap * n] compensation terms (mixed mode)
+    int* ncw;                        // wall contacts in history
+    int* hwid;                       // [hwcap * n] triangle index
+    typename T::real *hwx, *hwy, *hwz;
+    typename T::real *cwx, *cwy, *cwz;
 };
 
+// Contact law constants.  Linear: per-particle k and etaconst from the
+// material record (cpu_dem.cu:953).  Hertz-Mindlin (identical materials):
+// E* = E/(2(1-nu^2)), G* = E/(4(1+nu)(2-nu)), beta = ln e/sqrt(ln^2 e + pi^2);
+// kn = 4/3 E* sqrt(R* d), Sn = 2 E* sqrt(R* d), kt = St = 8 G* sqrt(R* d),
+// damping -2 sqrt(5/6) beta sqrt(S m*).
+struct Material {
+    int model;              // 0 linear, 1 Hertz-Mindlin
+    double mu;              // Coulomb coefficient
+    double kn_c;            // 4/3 E*
+    double sn_c;            // 2 E*
+    double kt_c;            // 8 G*
+    double damp_c;          // -2 sqrt(5/6) beta  (>= 0)
+    double mu_roll;         // rolling friction coefficient (0: off)
+};
+
+template <class T>
 struct View {
     int n;
-    SBank S[2];
-    PBank P[2];
+    SBank<T> S[2];
+    PBank<T> P[2];
     Ctl* ctl;
     // lists (rebuilt, not reordered)
     int *nei, *nnei, *neiw, *nneiw;
-    double *refx, *refy, *refz;
+    double4_32a* ref;                    // {x, y, z, -} at the last rebuild
     int nei_cap, wall_cap, hist_cap, histw_cap;
     // per-step force/torque output
     double *fx, *fy, *fz, *tx, *ty, *tz;
-    double* ftmp;        // [6 * n] scratch for reordering the force outputs
+    double* ftmp;                    // [6 * n] scratch for reordering the force outputs
     int store_forces;
     // sort scratch (ping-pong) and cell list
     uint32_t* keys[2];
     int* vals[2];
-    uint32_t* rs_hist;   // [256 * rs_blocks]
-    uint32_t* rs_tot;    // [256]
+    uint32_t* rs_hist;               // [256 * rs_blocks]
+    uint32_t* rs_tot;                // [256]
     int rs_blocks;
     int *cell_start, *cell_end;
     int ncells, sizex, sizey, sizez;
@@ -104,7 +138,8 @@ struct View {
     int ntri;
     int bvh_root;
     // scalars
-    double dt, mu;
+    Material mat;
+    double dt;
     double gx, gy, gz;
     double minx, miny, minz, maxx, maxy, maxz;
     double invdx, invdy, invdz;
@@ -259,23 +294,43 @@ __device__ __forceinline__ bool last_block(unsigned* counter) {
     return am_last;
 }
 
+// First slot of [0, n) whose bit is clear in `touched`, or n: the row length
+// update_history (cpu_dem.cu:587-609) leaves.  Its swap-with-last loop never
+// re-reads isContact after a swap, so every slot from the first lost contact
+// on is dropped.
+__device__ __forceinline__ int surviving(unsigned long long touched, int n) {
+    const unsigned long long lost = ~touched;
+    const int first = lost ? __ffsll((long long)lost) - 1 : 64;
+    return first < n ? first : n;
+}
+
 // ---------------------------------------------------------------- launchers
 // rebuild stages (gdem_rebuild.cu)
-void launch_rebuild(const View& v, cudaStream_t st, int n, int force);
-void launch_bvh_build(TriRec* tri, const double* aabb, BNode* nodes, const uint32_t* morton_sorted,
+template <class T>
+void launch_rebuild(const View<T>& v, cudaStream_t st, int force);
+template <class T>
+void launch_finalize_oob(const View<T>& v, cudaStream_t st);
+void launch_bvh_build(const double* aabb, BNode* nodes, const uint32_t* morton_sorted,
                       const int* sorted_idx, int* flags, int ntri, cudaStream_t st);
-void launch_tri_precompute(TriRec* rec, double* aabb, uint32_t* morton, int* idx, const double* vx,
+void launch_tri_precompute(TriRec* rec, uint32_t* morton, int* idx, const double* vx,
                            const double* vy, const double* vz, const int* tv, const int* te,
                            const double* raw3, int ntri, const double* gmin, const double* invrange,
                            cudaStream_t st);
 void radix_sort_pairs(uint32_t* keys0, int* vals0, uint32_t* keys1, int* vals1, uint32_t* hist,
                       uint32_t* tot, int n, int nblocks, int first_pass, int npasses, cudaStream_t st);
 int rs_blocks_for(int n);
-void launch_finalize_oob(const View& v, cudaStream_t st);
-// step kernels (gdem_step_fp64.cu)
-void launch_step_fp64(const View& v, cudaStream_t st, cudaGraphConditionalHandle cond, int use_cond);
-// exports and small utilities (gdem_rebuild.cu)
 void launch_dist_triangle(const TriRec* tri, const double* pos, const double* r, const int* t, int m,
                           double* out4, int* hit, cudaStream_t st);
+// step kernels (gdem_step_fp64.cu, gdem_step_mixed.cu)
+void launch_step(const View<FP64>& v, cudaStream_t st, cudaGraphConditionalHandle cond, int use_cond);
+void launch_step(const View<Mixed>& v, cudaStream_t st, cudaGraphConditionalHandle cond, int use_cond);
+void* step_kernel(const View<FP64>& v);
+void* step_kernel(const View<Mixed>& v);
+// stats and probes (gdem_stats.cu)
+template <class T>
+void launch_stats(const View<T>& v, double* partials, int nblk, cudaStream_t st);
+int stats_blocks(int n);
+template <class T>
+void launch_keys_probe(const View<T>& v, uint32_t* out, cudaStream_t st);
 
 }  // namespace gdem

@@ -176,41 +176,47 @@ void radix_sort_pairs(uint32_t* keys0, int* vals0, uint32_t* keys1, int* vals1, 
 // ===================================================================== keys
 // Morton key of every particle from its ghost-offset cell coordinates
 // (update_pList_withSort, BoundingBox.cu:680-690).  Inactive particles get an
-// all-ones key so they sort behind every cell.
-__global__ void k_keys(View v, int gated) {
+// all-ones key so they sort behind every cell; a particle leaving the box this
+// step (status 2) is still keyed, like the reference CPU loop still lists it.
+template <class T>
+__global__ void k_keys(View<T> v, int gated) {
     const Ctl* ctl = v.ctl;
     if (gated && ctl->refresh == 0u) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.n) return;
-    const SBank S = v.S[ctl->s];
+    const SBank<T> S = v.S[ctl->s];
     uint32_t key = kNoKey;
-    if (S.active[i] != 0) {  // 2 = leaving the box this step: still listed (main.cu:312-316)
-        const int cx = cell_coord(S.x[i], v.minx, v.invdx);
-        const int cy = cell_coord(S.y[i], v.miny, v.invdy);
-        const int cz = cell_coord(S.z[i], v.minz, v.invdz);
+    if (S.rot[i].w != 0) {
+        const double4_32a p = S.pos[i];
+        const int cx = cell_coord(p.x, v.minx, v.invdx);
+        const int cy = cell_coord(p.y, v.miny, v.invdy);
+        const int cz = cell_coord(p.z, v.minz, v.invdz);
         key = morton3((uint32_t)cx, (uint32_t)cy, (uint32_t)cz);
     }
     v.keys[0][i] = key;
     v.vals[0][i] = i;
 }
 
-// Deactivate particles that left the box at the last step (state 2 -> 0);
-// run before a rebuild requested between steps.
-__global__ void k_finalize_oob(View v) {
+// Deactivate particles that left the box at the last step (status 2 -> 0);
+// runs before a rebuild requested between steps.
+template <class T>
+__global__ void k_finalize_oob(View<T> v) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.n) return;
-    int* act = v.S[v.ctl->s].active;
-    if (act[i] == 2) act[i] = 0;
+    typename T::v4* rot = v.S[v.ctl->s].rot;
+    if (rot[i].w == 2) rot[i].w = 0;
 }
 
-void launch_finalize_oob(const View& v, cudaStream_t st) {
-    k_finalize_oob<<<(v.n + kBlock - 1) / kBlock, kBlock, 0, st>>>(v);
+template <class T>
+void launch_finalize_oob(const View<T>& v, cudaStream_t st) {
+    k_finalize_oob<T><<<(v.n + kBlock - 1) / kBlock, kBlock, 0, st>>>(v);
 }
 
 // ===================================================================== reorder
 // Gather every per-particle array into sorted order (d_swap_ps,
 // BoundingBox.cu:928-1005, but with compact histories: only live slots move).
-__global__ void k_reorder(View v, int gated) {
+template <class T>
+__global__ void k_reorder(View<T> v, int gated) {
     Ctl* ctl = v.ctl;
     if (gated && ctl->refresh == 0u) return;
     const int s = ctl->s, p = ctl->p;
@@ -218,26 +224,26 @@ __global__ void k_reorder(View v, int gated) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) {
         const int src = v.vals[0][i];
-        const SBank A = v.S[s], B = v.S[s ^ 1];
-        B.x[i] = A.x[src]; B.y[i] = A.y[src]; B.z[i] = A.z[src];
-        B.vx[i] = A.vx[src]; B.vy[i] = A.vy[src]; B.vz[i] = A.vz[src];
-        B.wx[i] = A.wx[src]; B.wy[i] = A.wy[src]; B.wz[i] = A.wz[src];
-        B.active[i] = A.active[src];
-        const PBank P = v.P[p], Q = v.P[p ^ 1];
-        Q.r[i] = P.r[src]; Q.rsq[i] = P.rsq[src]; Q.invm[i] = P.invm[src];
-        Q.sqrtm[i] = P.sqrtm[src]; Q.invmoi[i] = P.invmoi[src]; Q.k[i] = P.k[src];
-        Q.eta[i] = P.eta[src]; Q.pid[i] = P.pid[src];
+        const SBank<T> A = v.S[s], B = v.S[s ^ 1];
+        B.pos[i] = A.pos[src];
+        B.vel[i] = A.vel[src];
+        B.rot[i] = A.rot[src];
+        const PBank<T> P = v.P[p], Q = v.P[p ^ 1];
+        Q.mat[i] = P.mat[src];
+        Q.pid[i] = P.pid[src];
         const int nc = P.nc[src];
         Q.nc[i] = nc;
         for (int k = 0; k < nc; k++) {
             const size_t a = (size_t)k * n + src, b = (size_t)k * n + i;
             Q.hid[b] = P.hid[a]; Q.hx[b] = P.hx[a]; Q.hy[b] = P.hy[a]; Q.hz[b] = P.hz[a];
+            if (T::mixed) { Q.cx[b] = P.cx[a]; Q.cy[b] = P.cy[a]; Q.cz[b] = P.cz[a]; }
         }
         const int ncw = P.ncw[src];
         Q.ncw[i] = ncw;
         for (int k = 0; k < ncw; k++) {
             const size_t a = (size_t)k * n + src, b = (size_t)k * n + i;
             Q.hwid[b] = P.hwid[a]; Q.hwx[b] = P.hwx[a]; Q.hwy[b] = P.hwy[a]; Q.hwz[b] = P.hwz[a];
+            if (T::mixed) { Q.cwx[b] = P.cwx[a]; Q.cwy[b] = P.cwy[a]; Q.cwz[b] = P.cwz[a]; }
         }
     }
     if (last_block(&ctl->done[1])) {
@@ -250,7 +256,8 @@ __global__ void k_reorder(View v, int gated) {
 }
 
 // Per-step force/torque outputs follow the particles they belong to.
-__global__ void k_reorder_forces(View v, double* tmp, int gated) {
+template <class T>
+__global__ void k_reorder_forces(View<T> v, int gated) {
     const Ctl* ctl = v.ctl;
     if (gated && ctl->refresh == 0u) return;
     const int n = v.n;
@@ -258,20 +265,22 @@ __global__ void k_reorder_forces(View v, double* tmp, int gated) {
     if (i >= n) return;
     const int src = v.vals[0][i];
     double* f[6] = {v.fx, v.fy, v.fz, v.tx, v.ty, v.tz};
-    for (int c = 0; c < 6; c++) tmp[(size_t)c * n + i] = f[c][src];
+    for (int c = 0; c < 6; c++) v.ftmp[(size_t)c * n + i] = f[c][src];
 }
-__global__ void k_copy_forces(View v, const double* tmp, int gated) {
+template <class T>
+__global__ void k_copy_forces(View<T> v, int gated) {
     const Ctl* ctl = v.ctl;
     if (gated && ctl->refresh == 0u) return;
     const int n = v.n;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double* f[6] = {v.fx, v.fy, v.fz, v.tx, v.ty, v.tz};
-    for (int c = 0; c < 6; c++) f[c][i] = tmp[(size_t)c * n + i];
+    for (int c = 0; c < 6; c++) f[c][i] = v.ftmp[(size_t)c * n + i];
 }
 
 // ===================================================================== cells
-__global__ void k_cells_clear(View v, int gated) {
+template <class T>
+__global__ void k_cells_clear(View<T> v, int gated) {
     const Ctl* ctl = v.ctl;
     if (gated && ctl->refresh == 0u) return;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < v.ncells; c += gridDim.x * blockDim.x) {
@@ -283,7 +292,8 @@ __global__ void k_cells_clear(View v, int gated) {
 // Cell ranges from the sorted keys: equal keys are one cell, found by
 // comparing neighbours in the sorted order (no atomics; replaces
 // dk_build_cellCount + ExclusiveSum + dk_build_pList, BoundingBox.cu:1266).
-__global__ void k_cell_ranges(View v, int gated) {
+template <class T>
+__global__ void k_cell_ranges(View<T> v, int gated) {
     const Ctl* ctl = v.ctl;
     if (gated && ctl->refresh == 0u) return;
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
@@ -304,25 +314,26 @@ __global__ void k_cell_ranges(View v, int gated) {
 
 // ===================================================================== Verlet lists
 // One thread per particle: scan the 27 cells around its cell, keep every
-// active j != i with |xi - xj|^2 < (ri + rj + skin)^2 (the test of
-// BoundingBox.cu:1136-1144), order the row by the partner's pId (the
-// reference's index space) and record the reference position.
-template <int CAP>
-__global__ void __launch_bounds__(kBlock) k_neighbors(View v, int gated) {
+// listed j != i with |xi - xj|^2 < (ri + rj + skin)^2 (the test of
+// BoundingBox.cu:1136-1144, FP64 in every mode), order the row by the
+// partner's pId (the reference's index space) and record the reference
+// position.  Cells outside the grid hold nobody and are skipped.
+template <class T, int CAP>
+__global__ void __launch_bounds__(kBlock) k_neighbors(View<T> v, int gated) {
     Ctl* ctl = v.ctl;
     if (gated && ctl->refresh == 0u) return;
     const int n = v.n;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int s = ctl->s, p = ctl->p;
-    const SBank S = v.S[s];
-    const PBank P = v.P[p];
+    const SBank<T> S = v.S[s];
+    const PBank<T> P = v.P[p];
     int count = 0;
     if (i < n) {
-        if (S.active[i] == 0) {
+        if (S.rot[i].w == 0) {
             v.nnei[i] = 0;
         } else {
-            const double xi = S.x[i], yi = S.y[i], zi = S.z[i];
-            const double ri = P.r[i];
+            const double4_32a pi = S.pos[i];
+            const double xi = pi.x, yi = pi.y, zi = pi.z, ri = pi.w;
             const double skin = v.skin;
             const int cx = cell_coord(xi, v.minx, v.invdx);
             const int cy = cell_coord(yi, v.miny, v.invdy);
@@ -344,25 +355,26 @@ __global__ void __launch_bounds__(kBlock) k_neighbors(View v, int gated) {
                         for (int q = b; q < e; q++) {
                             const int j = v.reorder ? q : v.vals[0][q];
                             if (j == i) continue;
-                            const double dx = xi - S.x[j];
-                            const double dy = yi - S.y[j];
-                            const double dz = zi - S.z[j];
+                            const double4_32a pj = S.pos[j];
+                            const double dx = xi - pj.x;
+                            const double dy = yi - pj.y;
+                            const double dz = zi - pj.z;
                             const double distsq = dx * dx + dy * dy + dz * dz;
-                            const double R = ri + P.r[j] + skin;
+                            const double R = ri + pj.w + skin;
                             if (distsq < R * R) {
-                                const int pj = P.pid[j];
+                                const int pid_j = P.pid[j];
                                 if (count >= CAP) {
                                     overflow = true;
                                     continue;
                                 }
                                 // insertion by pId keeps the row sorted as it grows
                                 int k = count;
-                                while (k > 0 && cand_pid[k - 1] > pj) {
+                                while (k > 0 && cand_pid[k - 1] > pid_j) {
                                     cand_pid[k] = cand_pid[k - 1];
                                     cand_j[k] = cand_j[k - 1];
                                     k--;
                                 }
-                                cand_pid[k] = pj;
+                                cand_pid[k] = pid_j;
                                 cand_j[k] = j;
                                 count++;
                             }
@@ -374,12 +386,9 @@ __global__ void __launch_bounds__(kBlock) k_neighbors(View v, int gated) {
             const int m = count < v.nei_cap ? count : v.nei_cap;
             for (int k = 0; k < m; k++) v.nei[(size_t)k * n + i] = cand_j[k];
             v.nnei[i] = m;
-            v.refx[i] = xi;
-            v.refy[i] = yi;
-            v.refz[i] = zi;
+            v.ref[i] = make_double4_32a(xi, yi, zi, 0.0);
         }
     }
-    // longest row, for capacity reporting
     int wmax = count;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) wmax = max(wmax, __shfl_xor_sync(0xffffffffu, wmax, o));
@@ -393,22 +402,22 @@ __global__ void __launch_bounds__(kBlock) k_neighbors(View v, int gated) {
 // depend on the tree shape: an ancestor's box contains its leaves' boxes, so
 // the box test never rejects an ancestor of a leaf that passes.  Rows are
 // sorted by triangle index, as BVH.cu:538 does.
-template <int CAP>
-__global__ void __launch_bounds__(kBlock) k_wall_lists(View v, int gated) {
+template <class T, int CAP>
+__global__ void __launch_bounds__(kBlock) k_wall_lists(View<T> v, int gated) {
     Ctl* ctl = v.ctl;
     if (gated && ctl->refresh == 0u) return;
     const int n = v.n;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int s = ctl->s, p = ctl->p;
+    const int s = ctl->s;
     int count = 0;
     if (i < n) {
-        const SBank S = v.S[s];
-        const PBank P = v.P[p];
-        if (S.active[i] == 0 || v.ntri == 0) {
+        const SBank<T> S = v.S[s];
+        if (S.rot[i].w == 0 || v.ntri == 0) {
             v.nneiw[i] = 0;
         } else {
-            const double px = S.x[i], py = S.y[i], pz = S.z[i];
-            const double R = P.r[i] + v.skin;
+            const double4_32a pi = S.pos[i];
+            const double px = pi.x, py = pi.y, pz = pi.z;
+            const double R = pi.w + v.skin;
             const double Rsq = R * R;
             int cand[CAP];
             bool overflow = false;
@@ -422,7 +431,7 @@ __global__ void __launch_bounds__(kBlock) k_wall_lists(View v, int gated) {
                 if (B.tri >= 0) {
                     const int t = B.tri;
                     const Feature f = closest_feature(px, py, pz, Rsq, v.tri[t]);
-                    if (f.dist < P.r[i] + v.skin) {
+                    if (f.dist < pi.w + v.skin) {
                         if (count >= CAP) {
                             overflow = true;
                             continue;
@@ -467,35 +476,42 @@ __global__ void __launch_bounds__(kBlock) k_wall_lists(View v, int gated) {
 
 static inline int grid_for(int n) { return (n + kBlock - 1) / kBlock; }
 
-void launch_rebuild(const View& v, cudaStream_t st, int n, int force) {
+template <class T>
+void launch_rebuild(const View<T>& v, cudaStream_t st, int force) {
     const int gated = force ? 0 : 1;
+    const int n = v.n;
     const int g = grid_for(n);
-    k_keys<<<g, kBlock, 0, st>>>(v, gated);
+    k_keys<T><<<g, kBlock, 0, st>>>(v, gated);
     rs_passes(v.keys[0], v.vals[0], v.keys[1], v.vals[1], v.rs_hist, v.rs_tot, n, v.rs_blocks, 0, 4, st,
               v.ctl, gated);
     if (v.reorder) {
         if (v.store_forces) {
-            k_reorder_forces<<<g, kBlock, 0, st>>>(v, v.ftmp, gated);
-            k_copy_forces<<<g, kBlock, 0, st>>>(v, v.ftmp, gated);
+            k_reorder_forces<T><<<g, kBlock, 0, st>>>(v, gated);
+            k_copy_forces<T><<<g, kBlock, 0, st>>>(v, gated);
         }
-        k_reorder<<<g, kBlock, 0, st>>>(v, gated);
+        k_reorder<T><<<g, kBlock, 0, st>>>(v, gated);
     }
     const int gc = grid_for(v.ncells) < 4096 ? grid_for(v.ncells) : 4096;
-    k_cells_clear<<<gc, kBlock, 0, st>>>(v, gated);
-    k_cell_ranges<<<g, kBlock, 0, st>>>(v, gated);
+    k_cells_clear<T><<<gc, kBlock, 0, st>>>(v, gated);
+    k_cell_ranges<T><<<g, kBlock, 0, st>>>(v, gated);
     if (v.nei_cap <= 32)
-        k_neighbors<32><<<g, kBlock, 0, st>>>(v, gated);
+        k_neighbors<T, 32><<<g, kBlock, 0, st>>>(v, gated);
     else if (v.nei_cap <= 64)
-        k_neighbors<64><<<g, kBlock, 0, st>>>(v, gated);
+        k_neighbors<T, 64><<<g, kBlock, 0, st>>>(v, gated);
     else
-        k_neighbors<128><<<g, kBlock, 0, st>>>(v, gated);
+        k_neighbors<T, 128><<<g, kBlock, 0, st>>>(v, gated);
     if (v.wall_cap <= 16)
-        k_wall_lists<16><<<g, kBlock, 0, st>>>(v, gated);
+        k_wall_lists<T, 16><<<g, kBlock, 0, st>>>(v, gated);
     else if (v.wall_cap <= 32)
-        k_wall_lists<32><<<g, kBlock, 0, st>>>(v, gated);
+        k_wall_lists<T, 32><<<g, kBlock, 0, st>>>(v, gated);
     else
-        k_wall_lists<64><<<g, kBlock, 0, st>>>(v, gated);
+        k_wall_lists<T, 64><<<g, kBlock, 0, st>>>(v, gated);
 }
+
+template void launch_rebuild<FP64>(const View<FP64>&, cudaStream_t, int);
+template void launch_rebuild<Mixed>(const View<Mixed>&, cudaStream_t, int);
+template void launch_finalize_oob<FP64>(const View<FP64>&, cudaStream_t);
+template void launch_finalize_oob<Mixed>(const View<Mixed>&, cudaStream_t);
 
 // ===================================================================== mesh
 // Per-triangle precompute of load_ascii_stl_double (TriangleMesh.cu:560-630)
@@ -559,10 +575,10 @@ __global__ void k_tri_precompute(TriRec* rec, uint32_t* morton, int* idx, const 
     idx[t] = t;
 }
 
-void launch_tri_precompute(TriRec* rec, double* /*aabb*/, uint32_t* morton, int* idx,
-                           const double* vx, const double* vy, const double* vz, const int* tv,
-                           const int* te, const double* raw3, int ntri, const double* gmin,
-                           const double* invrange, cudaStream_t st) {
+void launch_tri_precompute(TriRec* rec, uint32_t* morton, int* idx, const double* vx,
+                           const double* vy, const double* vz, const int* tv, const int* te,
+                           const double* raw3, int ntri, const double* gmin, const double* invrange,
+                           cudaStream_t st) {
     if (ntri <= 0) return;
     k_tri_precompute<<<grid_for(ntri), kBlock, 0, st>>>(rec, morton, idx, vx, vy, vz, tv, te, raw3,
                                                         ntri, gmin[0], gmin[1], gmin[2], invrange[0],
@@ -649,9 +665,8 @@ __global__ void k_lbvh_init(BNode* nodes, int* flags, int n) {
     if (i < n) flags[i] = 0;
 }
 
-void launch_bvh_build(TriRec* /*tri*/, const double* aabb, BNode* nodes,
-                      const uint32_t* morton_sorted, const int* sorted_idx, int* flags, int ntri,
-                      cudaStream_t st) {
+void launch_bvh_build(const double* aabb, BNode* nodes, const uint32_t* morton_sorted,
+                      const int* sorted_idx, int* flags, int ntri, cudaStream_t st) {
     if (ntri <= 0) return;
     k_lbvh_init<<<grid_for(2 * ntri), kBlock, 0, st>>>(nodes, flags, ntri);
     if (ntri > 1) k_lbvh_internal<<<grid_for(ntri - 1), kBlock, 0, st>>>(nodes, morton_sorted, ntri);

@@ -1,8 +1,9 @@
 // Per-block reductions of the parity observables (kinetic energy, contact
-// and list counts, coordination, packing, maximum overlap) and the Morton-key
-// probe.  The reference has only an unused kineticEnergy (cpu_dem.cu:1554);
-// these reductions are deterministic: each block owns a fixed index range and
-// the host adds the block partials in block order.
+// and list counts, coordination, packing, maximum overlap), the Morton-key
+// probe and the pId-order position gather used by exports.  The reference has
+// only an unused kineticEnergy (cpu_dem.cu:1554); these reductions are
+// deterministic: each block owns a fixed index range and the host adds the
+// block partials in block order.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -18,21 +19,25 @@ int stats_blocks(int n) {
     return g < kStatBlocks ? (g > 0 ? g : 1) : kStatBlocks;
 }
 
-__global__ void __launch_bounds__(kBlock) k_stats(View v, double* partials) {
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_stats(View<T> v, double* partials) {
     const Ctl* ctl = v.ctl;
-    const SBank S = v.S[ctl->s];
-    const PBank P = v.P[ctl->p];
+    const SBank<T> S = v.S[ctl->s];
+    const PBank<T> P = v.P[ctl->p];
     double acc[kNStat];
     for (int k = 0; k < kNStat; k++) acc[k] = 0.;
     for (int k = 7; k < 10; k++) acc[k] = 1e300;
     for (int k = 10; k < 13; k++) acc[k] = -1e300;
     const int n = v.n;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        if (S.active[i] != 1) continue;
-        const double x = S.x[i], y = S.y[i], z = S.z[i], r = P.r[i];
-        const double m = 1. / P.invm[i], I = 1. / P.invmoi[i];
-        const double vv = S.vx[i] * S.vx[i] + S.vy[i] * S.vy[i] + S.vz[i] * S.vz[i];
-        const double ww = S.wx[i] * S.wx[i] + S.wy[i] * S.wy[i] + S.wz[i] * S.wz[i];
+        const auto w = S.rot[i];
+        if (w.w != 1) continue;
+        const double4_32a p = S.pos[i];
+        const auto ve = S.vel[i];
+        const double r = p.w;
+        const double m = 1. / (double)ve.w, I = 1. / (double)P.mat[i].w;
+        const double vv = (double)ve.x * ve.x + (double)ve.y * ve.y + (double)ve.z * ve.z;
+        const double ww = (double)w.x * w.x + (double)w.y * w.y + (double)w.z * w.z;
         acc[0] += 1.;
         acc[1] += v.nnei[i];
         acc[2] += v.nneiw[i];
@@ -40,18 +45,19 @@ __global__ void __launch_bounds__(kBlock) k_stats(View v, double* partials) {
         acc[4] += P.ncw[i];
         acc[5] += 0.5 * m * vv + 0.5 * I * ww;
         acc[6] += 4.0 / 3.0 * 3.141592653589793 * r * r * r;
-        acc[7] = fmin(acc[7], x - r);
-        acc[8] = fmin(acc[8], y - r);
-        acc[9] = fmin(acc[9], z - r);
-        acc[10] = fmax(acc[10], x + r);
-        acc[11] = fmax(acc[11], y + r);
-        acc[12] = fmax(acc[12], z + r);
+        acc[7] = fmin(acc[7], p.x - r);
+        acc[8] = fmin(acc[8], p.y - r);
+        acc[9] = fmin(acc[9], p.z - r);
+        acc[10] = fmax(acc[10], p.x + r);
+        acc[11] = fmax(acc[11], p.y + r);
+        acc[12] = fmax(acc[12], p.z + r);
         const int nn = v.nnei[i];
         for (int k = 0; k < nn; k++) {
             const int j = v.nei[(size_t)k * n + i];
-            if (S.active[j] != 1) continue;
-            const double dx = x - S.x[j], dy = y - S.y[j], dz = z - S.z[j];
-            const double R = r + P.r[j];
+            if (S.rot[j].w != 1) continue;
+            const double4_32a q = S.pos[j];
+            const double dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+            const double R = r + q.w;
             const double d2 = dx * dx + dy * dy + dz * dz;
             if (d2 < R * R) acc[13] = fmax(acc[13], (R - sqrt(d2)) / (2. * r));
         }
@@ -70,27 +76,56 @@ __global__ void __launch_bounds__(kBlock) k_stats(View v, double* partials) {
     if (threadIdx.x < kNStat) partials[16 * blockIdx.x + threadIdx.x] = sm[threadIdx.x][0];
 }
 
-void launch_stats(const View& v, double* partials, int nblk, cudaStream_t st) {
-    k_stats<<<nblk, kBlock, 0, st>>>(v, partials);
+template <class T>
+void launch_stats(const View<T>& v, double* partials, int nblk, cudaStream_t st) {
+    k_stats<T><<<nblk, kBlock, 0, st>>>(v, partials);
 }
 
-// Morton key of every stored particle into `out` (same formula as k_keys).
-__global__ void k_keys_probe(View v, uint32_t* out) {
+// Morton key of every stored particle into `out` (the formula of k_keys, for
+// particles active from the caller's point of view).
+template <class T>
+__global__ void k_keys_probe(View<T> v, uint32_t* out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.n) return;
-    const SBank S = v.S[v.ctl->s];
+    const SBank<T> S = v.S[v.ctl->s];
     uint32_t key = kNoKey;
-    if (S.active[i] == 1) {
-        const int cx = cell_coord(S.x[i], v.minx, v.invdx);
-        const int cy = cell_coord(S.y[i], v.miny, v.invdy);
-        const int cz = cell_coord(S.z[i], v.minz, v.invdz);
+    if (S.rot[i].w == 1) {
+        const double4_32a p = S.pos[i];
+        const int cx = cell_coord(p.x, v.minx, v.invdx);
+        const int cy = cell_coord(p.y, v.miny, v.invdy);
+        const int cz = cell_coord(p.z, v.minz, v.invdz);
         key = morton3((uint32_t)cx, (uint32_t)cy, (uint32_t)cz);
     }
     out[i] = key;
 }
 
-void launch_keys_probe(const View& v, uint32_t* out, cudaStream_t st) {
-    k_keys_probe<<<(v.n + kBlock - 1) / kBlock, kBlock, 0, st>>>(v, out);
+template <class T>
+void launch_keys_probe(const View<T>& v, uint32_t* out, cudaStream_t st) {
+    k_keys_probe<T><<<(v.n + kBlock - 1) / kBlock, kBlock, 0, st>>>(v, out);
 }
+
+// Positions in pId order, xyz-interleaved (the reference layout of x[]).
+template <class T>
+__global__ void k_gather_positions(View<T> v, double* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.n) return;
+    const double4_32a p = v.S[v.ctl->s].pos[i];
+    const int q = v.P[v.ctl->p].pid[i];
+    out[3 * (size_t)q + 0] = p.x;
+    out[3 * (size_t)q + 1] = p.y;
+    out[3 * (size_t)q + 2] = p.z;
+}
+
+template <class T>
+void launch_gather_positions(const View<T>& v, double* out, cudaStream_t st) {
+    k_gather_positions<T><<<(v.n + kBlock - 1) / kBlock, kBlock, 0, st>>>(v, out);
+}
+
+template void launch_stats<FP64>(const View<FP64>&, double*, int, cudaStream_t);
+template void launch_stats<Mixed>(const View<Mixed>&, double*, int, cudaStream_t);
+template void launch_keys_probe<FP64>(const View<FP64>&, uint32_t*, cudaStream_t);
+template void launch_keys_probe<Mixed>(const View<Mixed>&, uint32_t*, cudaStream_t);
+template void launch_gather_positions<FP64>(const View<FP64>&, double*, cudaStream_t);
+template void launch_gather_positions<Mixed>(const View<Mixed>&, double*, cudaStream_t);
 
 }  // namespace gdem

@@ -162,6 +162,14 @@ class Engine:
         self._check(self.L.gdem_export_particles(self.h, C.byref(p)), "gdem_export_particles")
         return out
 
+    def export_positions(self, out=None):
+        """Positions in pId order (x[3n], reference layout) with one device
+        gather and one transfer; `out` may be a pinned host array."""
+        x = np.empty(3 * self.n) if out is None else out
+        assert x.dtype == np.float64 and x.size == 3 * self.n and x.flags.c_contiguous
+        self._check(self.L.gdem_export_positions(self.h, _vp(x)), "gdem_export_positions")
+        return x
+
     def lists(self, stride=MAX_NEI):
         n = self.n
         nn = np.zeros(n, np.int32)

@@ -154,6 +154,11 @@ int gdem_synchronize(gdem_handle* h);   /* wait; GDEM_ERR_DEVICE if the error wo
 /* Download in pId order (replaces copyFromDevice, ParticleSystem.cu:97).
  * Fields left NULL are skipped. */
 int gdem_export_particles(gdem_handle* h, gdem_particles* p);
+
+/* Positions only, in pId order (x[3n], the SAVE_ON field write_frame_bin
+ * writes every output step, solver_output.cu:259): gathered on the device and
+ * copied with one transfer. */
+int gdem_export_positions(gdem_handle* h, double* x);
 int gdem_stats_get(gdem_handle* h, gdem_stats* s);
 
 /* ---- the hot-path stages, callable one at a time ---- */

@@ -96,7 +96,9 @@ struct Bvh {
 
 struct Contact {
     V3 fn, vn, vt, n;
-    double eta;
+    double eta;   // tangential damping (the linear law reuses the normal one)
+    double kt;    // tangential stiffness (the linear law uses k_i)
+    double Rstar; // effective radius (rolling resistance)
 };
 
 struct Feature {
@@ -108,6 +110,10 @@ struct Feature {
 struct Scene {
     int N = 0;
     double dt = 0., mu = 0., g[3] = {0, 0, 0};
+    // contact law: 0 linear (the reference's), 1 Hertz-Mindlin (restated from
+    // the published law; the reference has none)
+    int model = 0;
+    double kn_c = 0., sn_c = 0., kt_c = 0., damp_c = 0., mu_roll = 0.;
     std::vector<double> x, v, a, f, w, anga, mom, r, rsq, invr, k, m, sqrtm, invm, moi, invmoi, eta;
     std::vector<int> active, pId;
     std::vector<double> hx, hy, hz, hwx, hwy, hwz;
@@ -378,6 +384,10 @@ void plist(Scene& S) {
         if (S.active[i] != 1) continue;
         for (int a = 0; a < 3; a++) S.cellx[3 * i + a] = cell_of(S, S.x[3 * i + a], a);
         S.cellId[i] = (S.size[1] * S.cellx[3 * i + 2] + S.cellx[3 * i + 1]) * S.size[0] + S.cellx[3 * i];
+        if (S.cellId[i] < 0 || S.cellId[i] >= S.ncells) {
+            fprintf(stderr, "oracle: particle %d outside the cell grid\n", i);
+            abort();
+        }
         S.pNum[S.cellId[i]] += 1;
     }
     S.pStart[0] = 0;
@@ -414,6 +424,13 @@ bool build_lists(Scene& S) {
         for (int sx = -1; sx <= 1; sx++)
             for (int sy = -1; sy <= 1; sy++)
                 for (int sz = -1; sz <= 1; sz++) {
+                    // A particle leaving the box this step is still listed
+                    // (main.cu:312-316) and may sit in a ghost cell; the
+                    // reference then indexes outside its cell arrays.  Cells
+                    // outside the grid hold nobody, so they are skipped.
+                    if (cx + sx < 0 || cx + sx >= S.size[0] || cy + sy < 0 || cy + sy >= S.size[1] ||
+                        cz + sz < 0 || cz + sz >= S.size[2])
+                        continue;
                     const int c = (S.size[1] * (cz + sz) + cy + sy) * S.size[0] + cx + sx;
                     for (int q = S.pStart[c]; q < S.pStart[c] + S.pNum[c]; q++) {
                         const int j = S.pList[q];
@@ -485,14 +502,38 @@ bool build_lists(Scene& S) {
 }
 
 // ------------------------------------------------------------------ forces
+// Hertz normal force with Mindlin tangential stiffness for identical
+// materials (Tsuji et al. 1992; the damping of the usual DEM form):
+//   kn = 4/3 E* sqrt(R* d), Sn = 2 E* sqrt(R* d), kt = 8 G* sqrt(R* d),
+//   gamma = -2 sqrt(5/6) beta sqrt(S m*), beta = ln e / sqrt(ln^2 e + pi^2).
+// Same operation order as the engine's FP64 kernel.
+void hertz(const Scene& S, double Rstar, double mstar, double delMag, double vdn, V3 n, Contact& c) {
+    const double sqrtRd = sqrt(Rstar * delMag);
+    const double fel = S.kn_c * sqrtRd * delMag;
+    const double gn = S.damp_c * sqrt(S.sn_c * sqrtRd * mstar);
+    const double fnm = fel - gn * vdn;
+    c.fn = {fnm * n.x, fnm * n.y, fnm * n.z};
+    c.kt = S.kt_c * sqrtRd;
+    c.eta = S.damp_c * sqrt(c.kt * mstar);
+    c.Rstar = Rstar;
+}
+
 Contact normal_pp(Scene& S, int i, int j, V3 n, double delMag) {
     Contact c;
     const V3 del = scale(-delMag, n);
     const V3 vr{S.v[3 * i] - S.v[3 * j], S.v[3 * i + 1] - S.v[3 * j + 1], S.v[3 * i + 2] - S.v[3 * j + 2]};
-    c.vn = scale(dot(vr, n), n);
-    const double meff = 1. / (S.invm[i] + S.invm[j]);
-    c.eta = S.eta[i] * sqrt(meff);
-    c.fn = {-S.k[i] * del.x - c.eta * c.vn.x, -S.k[i] * del.y - c.eta * c.vn.y, -S.k[i] * del.z - c.eta * c.vn.z};
+    const double vdn = dot(vr, n);
+    c.vn = scale(vdn, n);
+    if (S.model == 1) {
+        hertz(S, S.r[i] * S.r[j] / (S.r[i] + S.r[j]), 1. / (S.invm[i] + S.invm[j]), delMag, vdn, n, c);
+    } else {
+        const double meff = 1. / (S.invm[i] + S.invm[j]);
+        c.eta = S.eta[i] * sqrt(meff);
+        c.kt = S.k[i];
+        c.Rstar = 0.;
+        c.fn = {-S.k[i] * del.x - c.eta * c.vn.x, -S.k[i] * del.y - c.eta * c.vn.y,
+                -S.k[i] * del.z - c.eta * c.vn.z};
+    }
     V3 rot{S.r[i] * S.w[3 * i] + S.r[j] * S.w[3 * j], S.r[i] * S.w[3 * i + 1] + S.r[j] * S.w[3 * j + 1],
            S.r[i] * S.w[3 * i + 2] + S.r[j] * S.w[3 * j + 2]};
     rot = cross(rot, n);
@@ -508,9 +549,17 @@ Contact normal_pw(Scene& S, int i, V3 n, double delMag) {
     Contact c;
     const V3 del = scale(-delMag, n);
     const V3 vr{S.v[3 * i], S.v[3 * i + 1], S.v[3 * i + 2]};
-    c.vn = scale(dot(vr, n), n);
-    c.eta = S.eta[i] * S.sqrtm[i];
-    c.fn = {-S.k[i] * del.x - c.eta * c.vn.x, -S.k[i] * del.y - c.eta * c.vn.y, -S.k[i] * del.z - c.eta * c.vn.z};
+    const double vdn = dot(vr, n);
+    c.vn = scale(vdn, n);
+    if (S.model == 1) {
+        hertz(S, S.r[i], 1. / S.invm[i], delMag, vdn, n, c);
+    } else {
+        c.eta = S.eta[i] * S.sqrtm[i];
+        c.kt = S.k[i];
+        c.Rstar = 0.;
+        c.fn = {-S.k[i] * del.x - c.eta * c.vn.x, -S.k[i] * del.y - c.eta * c.vn.y,
+                -S.k[i] * del.z - c.eta * c.vn.z};
+    }
     V3 rot{S.r[i] * S.w[3 * i], S.r[i] * S.w[3 * i + 1], S.r[i] * S.w[3 * i + 2]};
     rot = cross(rot, n);
     c.vt = add(sub(vr, c.vn), rot);
@@ -521,8 +570,9 @@ Contact normal_pw(Scene& S, int i, V3 n, double delMag) {
     return c;
 }
 
-// history spring update + Coulomb cap; `key` identifies the partner
-void tangential(Scene& S, int i, int key, const Contact& c, bool wall) {
+// history spring update + Coulomb cap; `key` identifies the partner; `wj`
+// is the partner's spin (null for a wall) for the rolling resistance
+void tangential(Scene& S, int i, int key, const Contact& c, bool wall, const double* wj) {
     const size_t ci = (size_t)i * K;
     int* id = wall ? S.hwid.data() : S.hid.data();
     int* flag = wall ? S.isCW.data() : S.isC.data();
@@ -548,13 +598,13 @@ void tangential(Scene& S, int i, int key, const Contact& c, bool wall) {
     const double dt = S.dt;
     V3 dn{hx[ci + slot] + c.vt.x * dt, hy[ci + slot] + c.vt.y * dt, hz[ci + slot] + c.vt.z * dt};
     dn = sub(dn, scale(dot(dn, c.n), c.n));
-    V3 ft = scale(-S.k[i], dn);
+    V3 ft = scale(-c.kt, dn);
     const double ftsq = dot(ft, ft), fnsq = dot(c.fn, c.fn);
     if (ftsq > (S.mu * S.mu) * fnsq) {
         if (ftsq != 0.) {
             const V3 t = scale(1. / (sqrt(ftsq) + 1e-15), ft);
             ft = scale(S.mu * sqrt(fnsq), t);
-            dn = scale(-1. / S.k[i], ft);
+            dn = scale(-1. / c.kt, ft);
         } else {
             ft = {0., 0., 0.};
         }
@@ -570,6 +620,18 @@ void tangential(Scene& S, int i, int key, const Contact& c, bool wall) {
     S.mom[3 * i] += mm.x;
     S.mom[3 * i + 1] += mm.y;
     S.mom[3 * i + 2] += mm.z;
+    if (S.model == 1 && S.mu_roll > 0.) {
+        // constant rolling resistance opposing the relative spin
+        const V3 rel = wj ? V3{S.w[3 * i] - wj[0], S.w[3 * i + 1] - wj[1], S.w[3 * i + 2] - wj[2]}
+                          : V3{S.w[3 * i], S.w[3 * i + 1], S.w[3 * i + 2]};
+        const double wn = sqrt(dot(rel, rel));
+        if (wn > 0.) {
+            const double tr = -S.mu_roll * c.Rstar * sqrt(fnsq) / wn;
+            S.mom[3 * i] += tr * rel.x;
+            S.mom[3 * i + 1] += tr * rel.y;
+            S.mom[3 * i + 2] += tr * rel.z;
+        }
+    }
     hx[ci + slot] = dn.x;
     hy[ci + slot] = dn.y;
     hz[ci + slot] = dn.z;
@@ -622,7 +684,7 @@ bool step(Scene& S) {
                 const double delMag = R - dist;
                 const V3 n{del.x / dist, del.y / dist, del.z / dist};
                 const Contact c = normal_pp(S, i, j, n, delMag);
-                tangential(S, i, S.pId[j], c, false);
+                tangential(S, i, S.pId[j], c, false, &S.w[3 * j]);
             }
         }
         compact(S, i, false);
@@ -649,7 +711,7 @@ bool step(Scene& S) {
                     }
                     const double delmag = S.r[i] - ff.dist;
                     const Contact c = normal_pw(S, i, ff.n, delmag);
-                    tangential(S, i, t, c, true);
+                    tangential(S, i, t, c, true, nullptr);
                 }
             }
             compact(S, i, true);
@@ -693,11 +755,23 @@ extern "C" {
 void* orc_create(int N, const double* x, const double* v, const double* w, const double* r, const double* m,
                  const double* k, const double* eta, double mu, double dt, const double* g, int nTri,
                  const double* tris, const int* files, int nfiles, const double* bmin, const double* bmax,
-                 double skin, double thresh) {
+                 double skin, double thresh, int model, double E, double nu, double e, double mu_roll) {
     Scene* S = new Scene();
     S->N = N;
     S->dt = dt;
     S->mu = mu;
+    S->model = model;
+    S->mu_roll = mu_roll;
+    if (model == 1) {
+        const double Es = E / (2. * (1. - nu * nu));
+        const double Gs = E / (4. * (1. + nu) * (2. - nu));
+        const double le = log(e);
+        const double beta = le / sqrt(le * le + M_PI * M_PI);
+        S->kn_c = 4. / 3. * Es;
+        S->sn_c = 2. * Es;
+        S->kt_c = 8. * Gs;
+        S->damp_c = -2. * sqrt(5. / 6.) * beta;
+    }
     for (int a = 0; a < 3; a++) S->g[a] = g[a];
     auto z = [&](std::vector<double>& a, size_t n) { a.assign(n, 0.); };
     for (auto* a : {&S->x, &S->v, &S->a, &S->f, &S->w, &S->anga, &S->mom}) z(*a, 3 * (size_t)N);

@@ -26,7 +26,8 @@ def lib():
         dp = C.POINTER(C.c_double)
         L.orc_create.restype = vp
         L.orc_create.argtypes = [C.c_int, vp, vp, vp, vp, vp, vp, vp, C.c_double, C.c_double, vp, C.c_int, vp,
-                                 vp, C.c_int, vp, vp, C.c_double, C.c_double]
+                                 vp, C.c_int, vp, vp, C.c_double, C.c_double, C.c_int, C.c_double, C.c_double,
+                                 C.c_double, C.c_double]
         L.orc_destroy.argtypes = [vp]
         L.orc_step.argtypes = [vp, C.c_int]
         L.orc_step.restype = C.c_int
@@ -59,7 +60,7 @@ _INT = {"isActive", "numCont", "numContWall", "indHis", "indHisWall", "numNei", 
 class OracleScene:
     """One scene in the CPU restatement of the reference (reference layout)."""
 
-    def __init__(self, sc, box=None, files=None):
+    def __init__(self, sc, box=None, files=None, model="linear"):
         from gpudem_gb300.engine import box_limits
         L = lib()
         self.sc = sc
@@ -82,7 +83,8 @@ class OracleScene:
         self.h = L.orc_create(self.N, _vp(x), _vp(v), _vp(w), _vp(arrs[0]), _vp(arrs[1]), _vp(arrs[2]),
                               _vp(arrs[3]), float(sc.mu), float(sc.dt), _vp(arrs[4]), self.nTri, _vp(tris),
                               _vp(fl), 0 if fl is None else fl.size, _vp(lo), _vp(hi), float(sc.skin),
-                              float(sc.refresh))
+                              float(sc.refresh), {"linear": 0, "hertz_mindlin": 1}[model], float(sc.E),
+                              float(sc.nu), float(sc.e), float(sc.mu_roll))
 
     def step(self, n=1):
         rc = lib().orc_step(self.h, int(n))

@@ -1,0 +1,109 @@
+"""Hertz-Mindlin (with rolling resistance) against the oracle's FP64
+restatement, and the mixed-precision mode against the FP64 engine.
+
+Hertz-Mindlin is not in the reference: its parity is against the oracle's
+restatement of the published law (oracle/gdem_oracle.cpp), bit for bit in
+FP64.  The mixed mode has no bit-level counterpart: its error is measured
+against the FP64 engine on the same inputs, with the tolerances written here.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import assert_rel, compact_rows
+
+pytestmark = pytest.mark.gpu
+
+# mixed-precision acceptance: positions after 1000 steps within 1e-4 r_min of
+# FP64; kinetic energy, coordination number and packing fraction within 0.5 %
+POS_TOL_RMIN = 1e-4
+OBS_RTOL = 5e-3
+
+
+def _hm_scene(n, seed, mu_roll=0.05):
+    from gpudem_gb300 import scenes
+    rng = np.random.default_rng(seed)
+    r0 = 2e-3
+    radii = r0 * rng.uniform(0.8, 1.2, n)
+    half = 0.1
+    s = half / 1.37
+    lo, hi = np.array([-s, -s, -s]), np.array([s, s, s])
+    x = scenes.lattice_packing(n, radii, lo, hi, rng, gap=0.02)
+    m = scenes.sphere_mass(2500.0, radii)
+    k = np.full(n, 2000.0)
+    return scenes.Scene(x=x, r=radii, m=m, k=k, eta=scenes.eta_const(k, 0.6), mu=0.4, dt=2e-6,
+                        tris=scenes.tilted_box_mesh(half, 30.0, 2), inlet_lo=lo, inlet_hi=hi,
+                        v=rng.normal(0.0, 0.5, (n, 3)), w=rng.normal(0.0, 40.0, (n, 3)),
+                        E=5e6, nu=0.3, e=0.6, mu_roll=mu_roll)
+
+
+@pytest.mark.parametrize("mu_roll", [0.0, 0.05])
+def test_hertz_mindlin_fp64_matches_oracle(mu_roll):
+    from gpudem_gb300 import engine
+    from oracle import port
+    sc = _hm_scene(20_000, seed=31, mu_roll=mu_roll)
+    E = engine.Engine(sc, model="hertz_mindlin", store_forces=True)
+    O = port.OracleScene(sc, model="hertz_mindlin")
+    done = 0
+    for c in (1, 50, 400):
+        E.step(c - done)
+        O.step(c - done)
+        done = c
+        st = E.export(history=True, forces=True)
+        assert np.array_equal(st["isActive"], O.get("isActive"))
+        nc, ncw = st["numCont"], st["numContWall"]
+        assert np.array_equal(nc, O.get("numCont")) and np.array_equal(ncw, O.get("numContWall"))
+        assert np.array_equal(compact_rows(st["indHis"], nc), compact_rows(O.get("indHis"), nc))
+        for nm in ("x", "v", "angv", "f", "mom"):
+            assert_rel(st[nm], O.get(nm), 1e-12, f"HM step {c} {nm}")
+        dh = np.stack([compact_rows(st["deltHis" + a], nc) for a in "xyz"])
+        dho = np.stack([compact_rows(O.get("deltHis" + a), nc) for a in "xyz"])
+        assert_rel(dh, dho, 1e-12, f"HM step {c} history")
+    s = E.stats()
+    assert s["error_word"] == 0 and s["n_contacts"] > 500
+
+
+@pytest.mark.parametrize("model", ["linear", "hertz_mindlin"])
+def test_mixed_close_to_fp64_small(model):
+    """20k spheres, 300 steps: mixed positions stay within 1e-4 r_min of FP64."""
+    from gpudem_gb300 import engine
+    sc = _hm_scene(20_000, seed=41)
+    A = engine.Engine(sc, precision="fp64", model=model)
+    B = engine.Engine(sc, precision="mixed", model=model)
+    A.step(300)
+    B.step(300)
+    xa = A.export(history=False)["x"]
+    xb = B.export(history=False)["x"]
+    err = np.max(np.abs(xa - xb))
+    assert err <= POS_TOL_RMIN * sc.r.min(), f"max position error {err:.3e} m"
+    sa, sb = A.stats(), B.stats()
+    assert sb["error_word"] == 0
+    assert abs(sb["kinetic_energy"] - sa["kinetic_energy"]) <= OBS_RTOL * sa["kinetic_energy"]
+
+
+def test_mixed_error_at_benchmark_size():
+    """The benchmark workload (1M lognormal spheres on the helical chute,
+    Hertz-Mindlin): after 1000 steps the mixed-precision positions are within
+    1e-4 r_min of the FP64 engine's, and kinetic energy, coordination number
+    and packing fraction agree to 0.5 %."""
+    from gpudem_gb300 import engine, scenes
+    sc = scenes.config3_helical_chute(n=1_000_000, v_sigma=0.5)
+    A = engine.Engine(sc, precision="fp64", model="hertz_mindlin")
+    A.step(1000)
+    xa = A.export(history=False)["x"]
+    sa = A.stats()
+    A.close()
+    B = engine.Engine(sc, precision="mixed", model="hertz_mindlin")
+    B.step(1000)
+    xb = B.export(history=False)["x"]
+    sb = B.stats()
+    B.close()
+    err = np.max(np.abs(xa - xb))
+    rmin = float(sc.r.min())
+    print(f"max |x_mixed - x_fp64| after 1000 steps = {err:.3e} m = {err / rmin:.2e} r_min; "
+          f"contacts fp64 {sa['n_contacts']} mixed {sb['n_contacts']}")
+    assert err <= POS_TOL_RMIN * rmin
+    for key in ("kinetic_energy", "packing_fraction"):
+        assert abs(sb[key] - sa[key]) <= OBS_RTOL * abs(sa[key]), key
+    assert abs(sb["coordination"] - sa["coordination"]) <= OBS_RTOL * max(sa["coordination"], 1e-9) + 1e-6
