@@ -219,9 +219,13 @@ def position_error(sc, kw, steps):
     B.step(steps)
     xb = B.export_positions()
     B.close()
-    err = float(np.max(np.abs(xa - xb)))
+    e = np.linalg.norm((xa - xb).reshape(-1, 3), axis=1)
     rmin = float(np.min(sc.r))
-    return {"pos_err_steps": steps, "pos_err_m": err, "pos_err_over_rmin": err / rmin}
+    return {"pos_err_steps": steps, "pos_err_max_over_rmin": float(e.max() / rmin),
+            "pos_err_p9999_over_rmin": float(np.percentile(e, 99.99) / rmin),
+            "pos_err_p99_over_rmin": float(np.percentile(e, 99) / rmin),
+            "pos_err_median_over_rmin": float(np.median(e) / rmin),
+            "pos_err_n_above_1e-4_rmin": int((e > 1e-4 * rmin).sum())}
 
 
 def run_e2e(args, sc, kw):

@@ -110,6 +110,7 @@ struct Impl : EngineBase {
         destroy_graphs();
         cudaFree(arena);
         cudaFree(cell_arena);
+        cudaFree(trif);
         if (st) cudaStreamDestroy(st);
     }
 
@@ -142,6 +143,12 @@ struct Impl : EngineBase {
             A.add(&S.pos, n);
             A.add(&S.vel, n);
             A.add(&S.rot, n);
+            if (T::mixed) {
+                A.add(&S.posh, n);
+                A.add(&S.posl, n);
+                A.add(&S.vell, n);
+                A.add(&S.rotl, n);
+            }
             PBank<T>& P = v.P[b];
             A.add(&P.mat, n);
             A.add(&P.pid, n);
@@ -161,6 +168,10 @@ struct Impl : EngineBase {
         A.add(&v.neiw, (size_t)n * v.wall_cap);
         A.add(&v.nneiw, n);
         A.add(&v.ref, n);
+        if (T::mixed) {
+            A.add(&v.refh, n);
+            A.add(&v.refl, n);
+        }
         if (v.store_forces) {
             A.add(&v.fx, n); A.add(&v.fy, n); A.add(&v.fz, n);
             A.add(&v.tx, n); A.add(&v.ty, n); A.add(&v.tz, n);
@@ -182,6 +193,10 @@ struct Impl : EngineBase {
         v.gz = d.g[2];
         v.minx = d.box_min[0]; v.miny = d.box_min[1]; v.minz = d.box_min[2];
         v.maxx = d.box_max[0]; v.maxy = d.box_max[1]; v.maxz = d.box_max[2];
+        for (int k = 0; k < 3; k++) {
+            v.boxf[k] = nextafterf((float)d.box_min[k], -INFINITY);
+            v.boxf[3 + k] = nextafterf((float)d.box_max[k], INFINITY);
+        }
         Material& m = v.mat;
         m.model = d.model;
         m.mu = d.mu;
@@ -200,12 +215,23 @@ struct Impl : EngineBase {
         return GDEM_OK;
     }
 
+    TriRecF* trif = nullptr;
+
     void set_mesh(const MeshData& M) override {
         destroy_graphs();
         v.ntri = M.ntri;
         v.tri = M.rec;
         v.bvh = M.nodes;
         v.bvh_root = 0;
+        if (T::mixed) {
+            cudaFree(trif);
+            trif = nullptr;
+            if (M.ntri > 0 && cudaMalloc((void**)&trif, sizeof(TriRecF) * M.ntri) == cudaSuccess) {
+                launch_trif(M.rec, trif, M.ntri, st);
+                cudaStreamSynchronize(st);
+            }
+            v.trif = trif;
+        }
     }
 
     int build_graph(int steps, cudaGraphExec_t* out) {
@@ -328,10 +354,42 @@ struct Impl : EngineBase {
         Cc.add(&v.cell_end, v.ncells);
         CKE(cudaMalloc((void**)&cell_arena, Cc.total()));
         Cc.bind(cell_arena);
+        std::vector<float4> posh, posl;
+        if (T::mixed) {
+            posh.resize(n);
+            posl.resize(n);
+            for (int i = 0; i < n; i++) {
+                const double xs[3] = {pos[i].x, pos[i].y, pos[i].z};
+                float hh[3], ll[3];
+                for (int k = 0; k < 3; k++) {
+                    hh[k] = (float)xs[k];
+                    ll[k] = (float)(xs[k] - (double)hh[k]);
+                }
+                posh[i] = make_float4(hh[0], hh[1], hh[2], (float)pos[i].w);
+                posl[i] = make_float4(ll[0], ll[1], ll[2], (float)rot[i].w);
+            }
+        }
         const SBank<T>& S = v.S[0];
         const PBank<T>& P = v.P[0];
 #define UP(dst, src, cnt) CKE(cudaMemcpyAsync(dst, src.data(), sizeof(src[0]) * (cnt), cudaMemcpyHostToDevice, st))
         UP(S.pos, pos, n); UP(S.vel, vel, n); UP(S.rot, rot, n);
+        if (T::mixed) {
+            UP(S.posh, posh, n);
+            UP(S.posl, posl, n);
+            std::vector<float4> vl(n), wl(n);
+            for (int i = 0; i < n; i++) {
+                // low parts of the velocity / spin pairs: input minus its FP32 rounding
+                const double vv[3] = {p->v ? p->v[3 * i] : 0., p->v ? p->v[3 * i + 1] : 0., p->v ? p->v[3 * i + 2] : 0.};
+                const double ww[3] = {p->angv ? p->angv[3 * i] : 0., p->angv ? p->angv[3 * i + 1] : 0.,
+                                      p->angv ? p->angv[3 * i + 2] : 0.};
+                vl[i] = make_float4((float)(vv[0] - (double)vel[i].x), (float)(vv[1] - (double)vel[i].y),
+                                    (float)(vv[2] - (double)vel[i].z), 0.f);
+                wl[i] = make_float4((float)(ww[0] - (double)rot[i].x), (float)(ww[1] - (double)rot[i].y),
+                                    (float)(ww[2] - (double)rot[i].z), 0.f);
+            }
+            UP(S.vell, vl, n);
+            UP(S.rotl, wl, n);
+        }
         UP(P.mat, mat, n); UP(P.pid, pid, n);
         UP(P.nc, nc, n); UP(P.hid, hid, (size_t)n * H);
         UP(P.hx, hx, (size_t)n * H); UP(P.hy, hy, (size_t)n * H); UP(P.hz, hz, (size_t)n * H);
@@ -426,11 +484,25 @@ struct Impl : EngineBase {
         if ((rc = dl(pos, S.pos, n)) || (rc = dl(vel, S.vel, n)) || (rc = dl(rot, S.rot, n)) ||
             (rc = dl(mat, P.mat, n)))
             return rc;
+        std::vector<float4> vl, wl;
+        if (T::mixed && ((rc = dl(vl, S.vell, n)) || (rc = dl(wl, S.rotl, n)))) return rc;
+        auto lo = [&](const std::vector<float4>& a, int i, int c) -> double {
+            if (!T::mixed) return 0.;
+            return c == 0 ? a[i].x : (c == 1 ? a[i].y : a[i].z);
+        };
         for (int i = 0; i < n; i++) {
             const int q = pid[i];
             if (p->x) { p->x[3 * q] = pos[i].x; p->x[3 * q + 1] = pos[i].y; p->x[3 * q + 2] = pos[i].z; }
-            if (p->v) { p->v[3 * q] = vel[i].x; p->v[3 * q + 1] = vel[i].y; p->v[3 * q + 2] = vel[i].z; }
-            if (p->angv) { p->angv[3 * q] = rot[i].x; p->angv[3 * q + 1] = rot[i].y; p->angv[3 * q + 2] = rot[i].z; }
+            if (p->v) {
+                p->v[3 * q] = (double)vel[i].x + lo(vl, i, 0);
+                p->v[3 * q + 1] = (double)vel[i].y + lo(vl, i, 1);
+                p->v[3 * q + 2] = (double)vel[i].z + lo(vl, i, 2);
+            }
+            if (p->angv) {
+                p->angv[3 * q] = (double)rot[i].x + lo(wl, i, 0);
+                p->angv[3 * q + 1] = (double)rot[i].y + lo(wl, i, 1);
+                p->angv[3 * q + 2] = (double)rot[i].z + lo(wl, i, 2);
+            }
             if (p->isActive) p->isActive[q] = rot[i].w == R(1) ? 1 : 0;
             if (p->r) p->r[q] = pos[i].w;
             if (p->m) p->m[q] = 1. / (double)vel[i].w;

@@ -58,6 +58,18 @@ struct __align__(16) BNode {
 };
 static_assert(sizeof(BNode) == 64, "BNode must be 64 bytes");
 
+// Mixed-mode copy of a triangle: the first corner as a float pair, the rest
+// in FP32 (128 bytes).
+struct __align__(16) TriRecF {
+    float v0h[3], v0l[3];
+    float n[3];
+    float e01[3], e02[3], e12[3];
+    float d00, d01, d11, denom, d00inv, d11inv, d22inv;
+    int i0, i1, i2, e0, e1, e2;
+    int pad;
+};
+static_assert(sizeof(TriRecF) == 128, "TriRecF must be 128 bytes");
+
 struct Ctl {
     int s;                    // state bank holding the current state
     int p;                    // property bank holding current properties/history
@@ -76,6 +88,15 @@ struct SBank {
     double4_32a* pos;
     typename T::v4* vel;
     typename T::v4* rot;
+    // mixed mode only: the positions as unevaluated float pairs x = hi + lo
+    // (hi = fl32(x), lo = fl32(x - hi)), which neighbours gather instead of
+    // pos, so a pair's relative vector is formed at FP64 accuracy with FP32
+    // adds: posh = {hi.xyz, r}, posl = {lo.xyz, status}
+    float4* posh;
+    float4* posl;
+    // mixed mode: low parts of the velocity and spin float pairs {lo.xyz, 0}
+    float4* vell;
+    float4* rotl;
 };
 
 // material record: linear model {k, etaconst, sqrt(m), 1/I};
@@ -118,6 +139,7 @@ struct View {
     // lists (rebuilt, not reordered)
     int *nei, *nnei, *neiw, *nneiw;
     double4_32a* ref;                    // {x, y, z, -} at the last rebuild
+    float4 *refh, *refl;             // mixed mode: the same as float pairs
     int nei_cap, wall_cap, hist_cap, histw_cap;
     // per-step force/torque output
     double *fx, *fy, *fz, *tx, *ty, *tz;
@@ -134,6 +156,7 @@ struct View {
     int reorder;
     // mesh
     const TriRec* tri;
+    const TriRecF* trif;             // mixed mode
     const BNode* bvh;
     int ntri;
     int bvh_root;
@@ -144,6 +167,7 @@ struct View {
     double minx, miny, minz, maxx, maxy, maxz;
     double invdx, invdy, invdz;
     double skin, thresh_sq;
+    float boxf[6];                   // mixed mode: box rounded outwards to FP32
 };
 
 // ---------------------------------------------------------------- Morton
@@ -321,6 +345,13 @@ void radix_sort_pairs(uint32_t* keys0, int* vals0, uint32_t* keys1, int* vals1, 
 int rs_blocks_for(int n);
 void launch_dist_triangle(const TriRec* tri, const double* pos, const double* r, const int* t, int m,
                           double* out4, int* hit, cudaStream_t st);
+void launch_trif(const TriRec* tri, TriRecF* out, int ntri, cudaStream_t st);
+
+// float pair split of an FP64 value: x == hi + lo to within 2^-48 |x|
+__device__ __forceinline__ void split2(double x, float& hi, float& lo) {
+    hi = __double2float_rn(x);
+    lo = __double2float_rn(x - (double)hi);
+}
 // step kernels (gdem_step_fp64.cu, gdem_step_mixed.cu)
 void launch_step(const View<FP64>& v, cudaStream_t st, cudaGraphConditionalHandle cond, int use_cond);
 void launch_step(const View<Mixed>& v, cudaStream_t st, cudaGraphConditionalHandle cond, int use_cond);

@@ -203,8 +203,11 @@ template <class T>
 __global__ void k_finalize_oob(View<T> v) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.n) return;
-    typename T::v4* rot = v.S[v.ctl->s].rot;
-    if (rot[i].w == 2) rot[i].w = 0;
+    const SBank<T> S = v.S[v.ctl->s];
+    if (S.rot[i].w == 2) {
+        S.rot[i].w = 0;
+        if (T::mixed) S.posl[i].w = 0.f;
+    }
 }
 
 template <class T>
@@ -228,6 +231,12 @@ __global__ void k_reorder(View<T> v, int gated) {
         B.pos[i] = A.pos[src];
         B.vel[i] = A.vel[src];
         B.rot[i] = A.rot[src];
+        if (T::mixed) {
+            B.posh[i] = A.posh[src];
+            B.posl[i] = A.posl[src];
+            B.vell[i] = A.vell[src];
+            B.rotl[i] = A.rotl[src];
+        }
         const PBank<T> P = v.P[p], Q = v.P[p ^ 1];
         Q.mat[i] = P.mat[src];
         Q.pid[i] = P.pid[src];
@@ -387,6 +396,20 @@ __global__ void __launch_bounds__(kBlock) k_neighbors(View<T> v, int gated) {
             for (int k = 0; k < m; k++) v.nei[(size_t)k * n + i] = cand_j[k];
             v.nnei[i] = m;
             v.ref[i] = make_double4_32a(xi, yi, zi, 0.0);
+            if (T::mixed) {
+                // reference position and a fresh float-pair split of the master
+                float4 h, l;
+                split2(xi, h.x, l.x);
+                split2(yi, h.y, l.y);
+                split2(zi, h.z, l.z);
+                h.w = l.w = 0.f;
+                v.refh[i] = h;
+                v.refl[i] = l;
+                h.w = (float)ri;
+                l.w = (float)S.rot[i].w;
+                S.posh[i] = h;
+                S.posl[i] = l;
+            }
         }
     }
     int wmax = count;
@@ -671,6 +694,31 @@ void launch_bvh_build(const double* aabb, BNode* nodes, const uint32_t* morton_s
     k_lbvh_init<<<grid_for(2 * ntri), kBlock, 0, st>>>(nodes, flags, ntri);
     if (ntri > 1) k_lbvh_internal<<<grid_for(ntri - 1), kBlock, 0, st>>>(nodes, morton_sorted, ntri);
     k_lbvh_refit<<<grid_for(ntri), kBlock, 0, st>>>(nodes, aabb, sorted_idx, flags, ntri);
+}
+
+// FP32 copy of the triangles for the mixed-precision step kernel.
+__global__ void k_trif(const TriRec* tri, TriRecF* out, int ntri) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntri) return;
+    const TriRec& T = tri[t];
+    TriRecF F;
+    for (int k = 0; k < 3; k++) {
+        split2(T.v0[k], F.v0h[k], F.v0l[k]);
+        F.n[k] = (float)T.n[k];
+        F.e01[k] = (float)T.e01[k];
+        F.e02[k] = (float)T.e02[k];
+        F.e12[k] = (float)T.e12[k];
+    }
+    F.d00 = (float)T.d00; F.d01 = (float)T.d01; F.d11 = (float)T.d11; F.denom = (float)T.denom;
+    F.d00inv = (float)T.d00inv; F.d11inv = (float)T.d11inv; F.d22inv = (float)T.d22inv;
+    F.i0 = T.i0; F.i1 = T.i1; F.i2 = T.i2; F.e0 = T.e0; F.e1 = T.e1; F.e2 = T.e2;
+    F.pad = 0;
+    out[t] = F;
+}
+
+void launch_trif(const TriRec* tri, TriRecF* out, int ntri, cudaStream_t st) {
+    if (ntri <= 0) return;
+    k_trif<<<grid_for(ntri), kBlock, 0, st>>>(tri, out, ntri);
 }
 
 // ===================================================================== probes

@@ -599,7 +599,8 @@ void tangential(Scene& S, int i, int key, const Contact& c, bool wall, const dou
     V3 dn{hx[ci + slot] + c.vt.x * dt, hy[ci + slot] + c.vt.y * dt, hz[ci + slot] + c.vt.z * dt};
     dn = sub(dn, scale(dot(dn, c.n), c.n));
     V3 ft = scale(-c.kt, dn);
-    const double ftsq = dot(ft, ft), fnsq = dot(c.fn, c.fn);
+    const double fnsq = dot(c.fn, c.fn);
+    const double ftsq = dot(ft, ft);
     if (ftsq > (S.mu * S.mu) * fnsq) {
         if (ftsq != 0.) {
             const V3 t = scale(1. / (sqrt(ftsq) + 1e-15), ft);
