@@ -32,6 +32,7 @@ UNITS = {
     "gdem_step_fp64.cu": True,
     "gdem_step_mixed.cu": False,
     "gdem_stats.cu": True,
+    "gdem_noalloc.cu": True,
 }
 
 

@@ -189,6 +189,24 @@ int gdem_export_cells(gdem_handle* h, uint32_t* keys_sorted, int* order, int* pN
  * device (radixSortUint32, BoundingBox.cu:33; CUB SortPairs, :1235). */
 int gdem_sort_keys(const uint32_t* keys, int n, uint32_t* keys_sorted, int* perm);
 
+/* Largest n gdem_sort_keys_noalloc accepts (its fixed device scratch is sized
+ * for this many keys: 8.5 MiB). */
+#define GDEM_SORT_NOALLOC_MAX_KEYS (1 << 20)
+
+/* The same stable sort as gdem_sort_keys with nothing allocated: d_keys,
+ * d_keys_sorted and d_perm are DEVICE pointers on the current device, and the
+ * work is enqueued on `stream` (a cudaStream_t; NULL = legacy default stream)
+ * without waiting for it.  The scratch is one fixed array per device, looked
+ * up on the first call on that device: make that first call before any stream
+ * capture begins.  Calls on one device must not overlap on the GPU (they share
+ * the scratch).  d_keys may equal d_keys_sorted; d_perm must not overlap
+ * either.  GDEM_ERR_CAPACITY when n > GDEM_SORT_NOALLOC_MAX_KEYS.
+ * No counterpart in the reference: it is for callers that must not allocate
+ * device memory while they run (a full device, a fixed memory budget, or a
+ * loop that cannot take the device-wide synchronisation of cudaFree). */
+int gdem_sort_keys_noalloc(const uint32_t* d_keys, int n, uint32_t* d_keys_sorted, int* d_perm,
+                           void* stream);
+
 /* Closest-feature test of m (sphere, triangle) pairs on the device
  * (dist_triangle, cpu_dem.cu:12 / device_dem.cu:12).  out4[4m] = n.xyz, dist;
  * hitAt[m] = -1 face, vertex id, or edge id + nShift; -2 when no contact. */
