@@ -20,10 +20,17 @@ EXPORTED = [
     "gdem_create", "gdem_destroy", "gdem_last_error", "gdem_set_mesh", "gdem_import_particles",
     "gdem_step", "gdem_synchronize", "gdem_export_particles", "gdem_stats_get", "gdem_rebuild",
     "gdem_export_lists", "gdem_morton_keys", "gdem_export_cells", "gdem_sort_keys",
-    "gdem_sort_keys_noalloc",
+    "gdem_sort_keys_noalloc", "gdem_set_mesh_indexed",
     "gdem_dist_triangle", "gdem_export_mesh", "gdem_get_stream", "gdem_profile_step",
     "gdem_export_positions",
 ]
+
+
+class MeshArrays(C.Structure):
+    """gdem_mesh_arrays: a welded mesh in the reference loader's arrays."""
+    _fields_ = [("nVert", C.c_int), ("nTri", C.c_int)] + [
+        (nm, C.c_void_p) for nm in ("mx", "my", "mz", "tri_i0", "tri_i1", "tri_i2",
+                                    "tri_e0", "tri_e1", "tri_e2", "d")]
 
 
 class Desc(C.Structure):
@@ -105,6 +112,7 @@ def load(build_if_missing: bool = False):
     L.gdem_export_cells.argtypes = [vp, vp, vp, vp, vp, vp, vp]
     L.gdem_sort_keys.argtypes = [vp, C.c_int, vp, vp]
     L.gdem_sort_keys_noalloc.argtypes = [vp, C.c_int, vp, vp, vp]
+    L.gdem_set_mesh_indexed.argtypes = [vp, C.POINTER(MeshArrays)]
     L.gdem_dist_triangle.argtypes = [vp, vp, vp, vp, C.c_int, vp, vp]
     L.gdem_export_mesh.argtypes = [vp, vp, vp, vp, vp, vp]
     L.gdem_get_stream.argtypes = [vp, C.POINTER(vp)]

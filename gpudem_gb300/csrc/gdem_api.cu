@@ -780,6 +780,10 @@ int gdem_destroy(gdem_handle* h) {
 }
 
 // ---------------------------------------------------------------- mesh
+static int upload_mesh(gdem_handle* h, const std::vector<double>& vx, const std::vector<double>& vy,
+                       const std::vector<double>& vz, const std::vector<int>& tv, const std::vector<int>& te,
+                       const double* raw3_h, const double* dplane_h, int T);
+
 int gdem_set_mesh(gdem_handle* h, const double* tris, int n_tri, const int* file_tri_counts, int nfiles) {
     if (!h || n_tri < 0 || (n_tri > 0 && !tris)) return fail(h, GDEM_ERR_ARG, "bad mesh arguments");
     cudaStream_t st = h->eng->st;
@@ -872,6 +876,18 @@ int gdem_set_mesh(gdem_handle* h, const double* tris, int n_tri, const int* file
         }
         t0 += f;
     }
+    return upload_mesh(h, vx, vy, vz, tv, te, raw3.data(), nullptr, T);
+}
+
+// Device half of the mesh set-up, shared by gdem_set_mesh (welded here) and
+// gdem_set_mesh_indexed (welded by the caller's loader): triangle and mesh
+// AABBs, per-triangle records, centroid keys, their sort and the LBVH.  The
+// plane offset comes from the raw third corner (raw3) or is given (dplane).
+static int upload_mesh(gdem_handle* h, const std::vector<double>& vx, const std::vector<double>& vy,
+                       const std::vector<double>& vz, const std::vector<int>& tv, const std::vector<int>& te,
+                       const double* raw3_h, const double* dplane_h, int T) {
+    cudaStream_t st = h->eng->st;
+    MeshData& M = h->mesh;
     // ---- triangle AABBs and the mesh AABB, in the loader's comparison order
     M.aabb_h.assign(6 * (size_t)T, 0.);
     double g[6] = {1e300, 1e300, 1e300, -1e300, -1e300, -1e300};
@@ -906,7 +922,7 @@ int gdem_set_mesh(gdem_handle* h, const double* tris, int n_tri, const int* file
     A.add(&M.nodes, 2 * (size_t)T);
     A.add(&M.aabb_d, 6 * (size_t)T);
     A.add(&dvx, NV); A.add(&dvy, NV); A.add(&dvz, NV);
-    A.add(&draw3, 3 * (size_t)T);
+    A.add(&draw3, raw3_h ? 3 * (size_t)T : (size_t)T);
     A.add(&dtv, 3 * (size_t)T); A.add(&dte, 3 * (size_t)T);
     A.add(&flags, T);
     A.add(&M.morton[0], T); A.add(&M.morton[1], T);
@@ -919,11 +935,15 @@ int gdem_set_mesh(gdem_handle* h, const double* tris, int n_tri, const int* file
     CK(cudaMemcpyAsync(dvx, vx.data(), sizeof(double) * NV, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(dvy, vy.data(), sizeof(double) * NV, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(dvz, vz.data(), sizeof(double) * NV, cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(draw3, raw3.data(), sizeof(double) * 3 * T, cudaMemcpyHostToDevice, st));
+    if (raw3_h)
+        CK(cudaMemcpyAsync(draw3, raw3_h, sizeof(double) * 3 * T, cudaMemcpyHostToDevice, st));
+    else
+        CK(cudaMemcpyAsync(draw3, dplane_h, sizeof(double) * T, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(dtv, tv.data(), sizeof(int) * 3 * T, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(dte, te.data(), sizeof(int) * 3 * T, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(M.aabb_d, M.aabb_h.data(), sizeof(double) * 6 * T, cudaMemcpyHostToDevice, st));
-    launch_tri_precompute(M.rec, M.morton[0], M.idx[0], dvx, dvy, dvz, dtv, dte, draw3, T, g, inv, st);
+    launch_tri_precompute(M.rec, M.morton[0], M.idx[0], dvx, dvy, dvz, dtv, dte, raw3_h ? draw3 : nullptr,
+                          raw3_h ? nullptr : draw3, T, g, inv, st);
     // stable sort of the centroid keys (radixSortUint32 at TriangleMesh.cu:722)
     radix_sort_pairs(M.morton[0], M.idx[0], M.morton[1], M.idx[1], hist, tot, T, nb, 0, 4, st);
     launch_bvh_build(M.aabb_d, M.nodes, M.morton[0], M.idx[0], flags, T, st);
@@ -932,6 +952,32 @@ int gdem_set_mesh(gdem_handle* h, const double* tris, int n_tri, const int* file
     h->eng->set_mesh(M);
     if (h->eng->imported) return pass(h, h->eng->rebuild());
     return GDEM_OK;
+}
+
+int gdem_set_mesh_indexed(gdem_handle* h, const gdem_mesh_arrays* m) {
+    if (!h || !m || m->nTri < 0 || m->nVert < 0) return fail(h, GDEM_ERR_ARG, "bad mesh arguments");
+    const int T = m->nTri, NV = m->nVert;
+    if (T > 0 && (!m->mx || !m->my || !m->mz || !m->tri_i0 || !m->tri_i1 || !m->tri_i2 || !m->tri_e0 ||
+                  !m->tri_e1 || !m->tri_e2 || !m->d))
+        return fail(h, GDEM_ERR_ARG, "mesh arrays missing");
+    cudaStreamSynchronize(h->eng->st);
+    MeshData& M = h->mesh;
+    cudaFree(M.arena);
+    M = MeshData();
+    if (T == 0) {
+        h->eng->set_mesh(M);
+        return h->eng->imported ? pass(h, h->eng->rebuild()) : GDEM_OK;
+    }
+    std::vector<double> vx(m->mx, m->mx + NV), vy(m->my, m->my + NV), vz(m->mz, m->mz + NV);
+    std::vector<int> tv(3 * (size_t)T), te(3 * (size_t)T);
+    for (int t = 0; t < T; t++) {
+        const int a = m->tri_i0[t], b = m->tri_i1[t], c = m->tri_i2[t];
+        // the loader stores each triangle's vertex ids ascending (sort3, TriangleMesh.cu:89-103)
+        if (a < 0 || c >= NV || a > b || b > c) return fail(h, GDEM_ERR_ARG, "need 0 <= tri_i0 <= tri_i1 <= tri_i2 < nVert");
+        tv[3 * t] = a; tv[3 * t + 1] = b; tv[3 * t + 2] = c;
+        te[3 * t] = m->tri_e0[t]; te[3 * t + 1] = m->tri_e1[t]; te[3 * t + 2] = m->tri_e2[t];
+    }
+    return upload_mesh(h, vx, vy, vz, tv, te, nullptr, m->d, T);
 }
 
 int gdem_export_mesh(gdem_handle* h, double* rec, int* irec, double* aabb, uint32_t* morton, int* sorted_index) {

@@ -338,8 +338,8 @@ void launch_bvh_build(const double* aabb, BNode* nodes, const uint32_t* morton_s
                       const int* sorted_idx, int* flags, int ntri, cudaStream_t st);
 void launch_tri_precompute(TriRec* rec, uint32_t* morton, int* idx, const double* vx,
                            const double* vy, const double* vz, const int* tv, const int* te,
-                           const double* raw3, int ntri, const double* gmin, const double* invrange,
-                           cudaStream_t st);
+                           const double* raw3, const double* dplane, int ntri, const double* gmin,
+                           const double* invrange, cudaStream_t st);
 void radix_sort_pairs(uint32_t* keys0, int* vals0, uint32_t* keys1, int* vals1, uint32_t* hist,
                       uint32_t* tot, int n, int nblocks, int first_pass, int npasses, cudaStream_t st);
 int rs_blocks_for(int n);

@@ -539,11 +539,12 @@ template void launch_finalize_oob<Mixed>(const View<Mixed>&, cudaStream_t);
 // ===================================================================== mesh
 // Per-triangle precompute of load_ascii_stl_double (TriangleMesh.cu:560-630)
 // from welded vertices (tv = sorted vertex ids, te = edge ids + nShift) and
-// the raw third corner (the plane offset uses it, TriangleMesh.cu:607), plus
-// the centroid Morton key of mortonKeyGen (TriangleMesh.cu:4-21).
+// the raw third corner (the plane offset uses it, TriangleMesh.cu:607) or,
+// when raw3 is null, the plane offsets the loader already computed (dplane),
+// plus the centroid Morton key of mortonKeyGen (TriangleMesh.cu:4-21).
 __global__ void k_tri_precompute(TriRec* rec, uint32_t* morton, int* idx, const double* vx,
                                  const double* vy, const double* vz, const int* tv, const int* te,
-                                 const double* raw3, int ntri, double gminx, double gminy,
+                                 const double* raw3, const double* dplane, int ntri, double gminx, double gminy,
                                  double gminz, double irx, double iry, double irz) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ntri) return;
@@ -579,8 +580,12 @@ __global__ void k_tri_precompute(TriRec* rec, uint32_t* morton, int* idx, const 
     R.n[0] = nx;
     R.n[1] = ny;
     R.n[2] = nz;
-    const double x = raw3[3 * t + 0], y = raw3[3 * t + 1], z = raw3[3 * t + 2];
-    R.d = -nx * x - ny * y - nz * z;
+    if (raw3) {
+        const double x = raw3[3 * t + 0], y = raw3[3 * t + 1], z = raw3[3 * t + 2];
+        R.d = -nx * x - ny * y - nz * z;
+    } else {
+        R.d = dplane[t];
+    }
     R.i0 = a;
     R.i1 = b;
     R.i2 = c;
@@ -600,10 +605,10 @@ __global__ void k_tri_precompute(TriRec* rec, uint32_t* morton, int* idx, const 
 
 void launch_tri_precompute(TriRec* rec, uint32_t* morton, int* idx, const double* vx,
                            const double* vy, const double* vz, const int* tv, const int* te,
-                           const double* raw3, int ntri, const double* gmin, const double* invrange,
-                           cudaStream_t st) {
+                           const double* raw3, const double* dplane, int ntri, const double* gmin,
+                           const double* invrange, cudaStream_t st) {
     if (ntri <= 0) return;
-    k_tri_precompute<<<grid_for(ntri), kBlock, 0, st>>>(rec, morton, idx, vx, vy, vz, tv, te, raw3,
+    k_tri_precompute<<<grid_for(ntri), kBlock, 0, st>>>(rec, morton, idx, vx, vy, vz, tv, te, raw3, dplane,
                                                         ntri, gmin[0], gmin[1], gmin[2], invrange[0],
                                                         invrange[1], invrange[2]);
 }

@@ -100,6 +100,21 @@ class Engine:
         self._check(self.L.gdem_set_mesh(self.h, _vp(t), self.ntri, _vp(fc), 0 if fc is None else fc.size),
                     "gdem_set_mesh")
 
+    def set_mesh_indexed(self, mx, my, mz, tri_i, tri_e, d):
+        """Mesh from a loader's welded arrays (gdem_set_mesh_indexed): vertex
+        coordinates, per-triangle vertex ids [T,3] (ascending), edge ids + nShift
+        [T,3] and plane offsets d [T]."""
+        keep = [np.ascontiguousarray(a, np.float64) for a in (mx, my, mz, d)]
+        ti = np.ascontiguousarray(np.asarray(tri_i, np.int32).reshape(-1, 3).T)
+        te = np.ascontiguousarray(np.asarray(tri_e, np.int32).reshape(-1, 3).T)
+        m = _lib.MeshArrays()
+        m.nVert, m.nTri = keep[0].size, ti.shape[1]
+        m.mx, m.my, m.mz, m.d = (_vp(a) for a in keep)
+        m.tri_i0, m.tri_i1, m.tri_i2 = (_vp(ti[c]) for c in range(3))
+        m.tri_e0, m.tri_e1, m.tri_e2 = (_vp(te[c]) for c in range(3))
+        self.ntri = m.nTri
+        self._check(self.L.gdem_set_mesh_indexed(self.h, C.byref(m)), "gdem_set_mesh_indexed")
+
     def import_particles(self, sc: Scene, history=None):
         n = sc.n
         self._keep = []

@@ -139,6 +139,24 @@ const char* gdem_last_error(gdem_handle* h);   /* message of the last failing ca
 int gdem_set_mesh(gdem_handle* h, const double* tris, int n_tri, const int* file_tri_counts,
                   int nfiles);
 
+/* A mesh the reference's loader has already welded, in its own arrays
+ * (TriangleMesh.h:102-170, filled by load_ascii_stl_double,
+ * TriangleMesh.cu:363-752).  Vertex ids per triangle ascending, edge ids with
+ * nShift already added, d the plane offsets the loader computed. */
+typedef struct gdem_mesh_arrays {
+    int nVert, nTri;
+    const double *mx, *my, *mz;              /* [nVert] vertex coordinates */
+    const int *tri_i0, *tri_i1, *tri_i2;     /* [nTri] vertex ids, tri_i0 <= tri_i1 <= tri_i2 */
+    const int *tri_e0, *tri_e1, *tri_e2;     /* [nTri] edge ids + nShift */
+    const double* d;                         /* [nTri] plane offset -n.x */
+} gdem_mesh_arrays;
+
+/* Wall mesh from the reference's loaded TriangleMesh arrays: the same device
+ * records, keys and BVH as gdem_set_mesh builds from the STL corners that
+ * loader read, without welding again.  This is the call a reference host
+ * makes after load_ascii_stl_double (main.cu:99). */
+int gdem_set_mesh_indexed(gdem_handle* h, const gdem_mesh_arrays* m);
+
 /* Upload particles (replaces copyToDevice, ParticleSystem.cu:82).  Builds the
  * Verlet and wall lists from the imported state (main.cu:152,199 do this on the
  * host in the reference). */

@@ -72,10 +72,13 @@ MESH_FIELDS = ["nx", "ny", "nz", "d", None, None, None, None, None, None, None, 
                "d00", "d01", "d11", "denom", "d00inv", "d11inv", "d22inv"]
 
 
+@pytest.mark.parametrize("ingest", ["corners", "indexed"])
 @pytest.mark.parametrize("case", ["tilted", "chute", "box"])
-def test_mesh_precompute_and_wall_lists(eng_mod, case):
+def test_mesh_precompute_and_wall_lists(eng_mod, case, ingest):
     """load_ascii_stl_double precompute (TriangleMesh.cu:560-722), dist_triangle
-    (cpu_dem.cu:12) and the wall lists (BVH.cu:576) of probe spheres."""
+    (cpu_dem.cu:12) and the wall lists (BVH.cu:576) of probe spheres, with the
+    mesh given as STL corners (welded by the engine) or as the reference
+    loader's own welded arrays (gdem_set_mesh_indexed)."""
     from gpudem_gb300.scenes import Scene, eta_const, sphere_mass
     g = load_golden("meshes")
     tris = g[f"{case}_tris"]
@@ -87,6 +90,10 @@ def test_mesh_precompute_and_wall_lists(eng_mod, case):
                mu=0.5, dt=1e-5, tris=tris, inlet_lo=lo_in, inlet_hi=lo_in + 0.02)
     box_d = g[f"{case}_box_d"]
     E = eng_mod.Engine(sc, box=(box_d[0:3], box_d[3:6]))
+    if ingest == "indexed":
+        E.set_mesh_indexed(g[f"{case}_mx"], g[f"{case}_my"], g[f"{case}_mz"],
+                           np.stack([g[f"{case}_tri_i{c}"] for c in range(3)], 1),
+                           np.stack([g[f"{case}_tri_e{c}"] for c in range(3)], 1), g[f"{case}_d"])
     rec, irec, aabb, mort, idx = E.mesh()
     for c, f in enumerate(MESH_FIELDS):
         if f is not None:
