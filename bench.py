@@ -193,7 +193,8 @@ def run_engine(args):
         "clocks": clk.summary(),
         # one step kernel per step + the rebuild kernels of each rebuild
         # (keys, 4 x 3 sort passes, reorder, cell clear, cell ranges, Verlet, walls)
-        "gpu_launches": args.steps + reb * 18,
+        # (+ the FP32 position copy of the FP64 mode's list prefilter)
+        "gpu_launches": args.steps + reb * (18 if mixed else 19),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": args.traffic,
                      "peak_kind": f"{peak_kind} hbm_gbs",

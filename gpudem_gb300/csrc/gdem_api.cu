@@ -140,7 +140,7 @@ struct Impl : EngineBase {
         Arena A;
         for (int b = 0; b < 2; b++) {
             SBank<T>& S = v.S[b];
-            A.add(&S.pos, n);
+            if (!T::mixed) A.add(&S.pos, n);
             A.add(&S.vel, n);
             A.add(&S.rot, n);
             if (T::mixed) {
@@ -167,10 +167,11 @@ struct Impl : EngineBase {
         A.add(&v.nnei, n);
         A.add(&v.neiw, (size_t)n * v.wall_cap);
         A.add(&v.nneiw, n);
-        A.add(&v.ref, n);
         if (T::mixed) {
             A.add(&v.refh, n);
-            A.add(&v.refl, n);
+        } else {
+            A.add(&v.ref, n);
+            A.add(&v.posf, n);
         }
         if (v.store_forces) {
             A.add(&v.fx, n); A.add(&v.fy, n); A.add(&v.fz, n);
@@ -193,10 +194,19 @@ struct Impl : EngineBase {
         v.gz = d.g[2];
         v.minx = d.box_min[0]; v.miny = d.box_min[1]; v.minz = d.box_min[2];
         v.maxx = d.box_max[0]; v.maxy = d.box_max[1]; v.maxz = d.box_max[2];
+        float xmax = 0.f;
         for (int k = 0; k < 3; k++) {
             v.boxf[k] = nextafterf((float)d.box_min[k], -INFINITY);
             v.boxf[3 + k] = nextafterf((float)d.box_max[k], INFINITY);
+            xmax = fmaxf(xmax, fmaxf(fabsf(v.boxf[k]), fabsf(v.boxf[3 + k])));
         }
+        // a particle still listed while leaving the box lies within twice the
+        // largest box coordinate; 8 ulps there bound the FP32 distance error
+        v.nb_delta = 8.f * (nextafterf(2.f * xmax, INFINITY) - 2.f * xmax);
+        v.dtf = (float)d.dt;
+        v.gxf = (float)d.g[0];
+        v.gyf = (float)d.g[1];
+        v.gzf = (float)d.g[2];
         Material& m = v.mat;
         m.model = d.model;
         m.mu = d.mu;
@@ -212,6 +222,12 @@ struct Impl : EngineBase {
             m.kt_c = 8. * Gs;
             m.damp_c = -2. * sqrt(5. / 6.) * beta;
         }
+        v.muf = (float)m.mu;
+        v.kn_cf = (float)m.kn_c;
+        v.sn_cf = (float)m.sn_c;
+        v.kt_cf = (float)m.kt_c;
+        v.damp_cf = (float)m.damp_c;
+        v.mu_rollf = (float)m.mu_roll;
         return GDEM_OK;
     }
 
@@ -238,18 +254,17 @@ struct Impl : EngineBase {
         cudaGraph_t g;
         CKE(cudaGraphCreate(&g, 0));
         cudaGraphNode_t prev = nullptr;
-        const int grid = (n + kBlock - 1) / kBlock;
-        void* fn = step_kernel(v);
+        const StepLaunch L = step_launch(v);
         for (int k = 0; k < steps; k++) {
             cudaGraphConditionalHandle hnd;
             CKE(cudaGraphConditionalHandleCreate(&hnd, g, 0, cudaGraphCondAssignDefault));
             int use_cond = 1;
             void* args[3] = {(void*)&v, (void*)&hnd, (void*)&use_cond};
             cudaKernelNodeParams kp = {};
-            kp.func = fn;
-            kp.gridDim = dim3(grid);
-            kp.blockDim = dim3(kBlock);
-            kp.sharedMemBytes = 0;
+            kp.func = L.fn;
+            kp.gridDim = L.grid;
+            kp.blockDim = L.block;
+            kp.sharedMemBytes = (unsigned)L.smem;
             kp.kernelParams = args;
             cudaGraphNode_t sn;
             CKE(cudaGraphAddKernelNode(&sn, g, prev ? &prev : nullptr, prev ? 1 : 0, &kp));
@@ -340,6 +355,7 @@ struct Impl : EngineBase {
             return failv(err, GDEM_ERR_ARG, "cell size smaller than the largest list cutoff 2*r_max+skin");
         v.skin = skin;
         v.thresh_sq = thresh * thresh;
+        v.thresh_sqf = (float)v.thresh_sq;
         v.invdx = v.invdy = v.invdz = 1. / cell;
         v.sizex = (int)ceil((v.maxx - v.minx) / cell) + 2;
         v.sizey = (int)ceil((v.maxy - v.miny) / cell) + 2;
@@ -372,7 +388,8 @@ struct Impl : EngineBase {
         const SBank<T>& S = v.S[0];
         const PBank<T>& P = v.P[0];
 #define UP(dst, src, cnt) CKE(cudaMemcpyAsync(dst, src.data(), sizeof(src[0]) * (cnt), cudaMemcpyHostToDevice, st))
-        UP(S.pos, pos, n); UP(S.vel, vel, n); UP(S.rot, rot, n);
+        if (!T::mixed) UP(S.pos, pos, n);
+        UP(S.vel, vel, n); UP(S.rot, rot, n);
         if (T::mixed) {
             UP(S.posh, posh, n);
             UP(S.posl, posl, n);
@@ -481,9 +498,17 @@ struct Impl : EngineBase {
         const PBank<T>& P = v.P[c.p];
         std::vector<double4_32a> pos;
         std::vector<V4> vel, rot, mat;
-        if ((rc = dl(pos, S.pos, n)) || (rc = dl(vel, S.vel, n)) || (rc = dl(rot, S.rot, n)) ||
-            (rc = dl(mat, P.mat, n)))
+        if ((rc = dl(vel, S.vel, n)) || (rc = dl(rot, S.rot, n)) || (rc = dl(mat, P.mat, n))) return rc;
+        if (T::mixed) {
+            std::vector<float4> ph, pl;
+            if ((rc = dl(ph, S.posh, n)) || (rc = dl(pl, S.posl, n))) return rc;
+            pos.resize(n);
+            for (int i = 0; i < n; i++)
+                pos[i] = make_double4_32a((double)ph[i].x + (double)pl[i].x, (double)ph[i].y + (double)pl[i].y,
+                                          (double)ph[i].z + (double)pl[i].z, (double)ph[i].w);
+        } else if ((rc = dl(pos, S.pos, n))) {
             return rc;
+        }
         std::vector<float4> vl, wl;
         if (T::mixed && ((rc = dl(vl, S.vell, n)) || (rc = dl(wl, S.rotl, n)))) return rc;
         auto lo = [&](const std::vector<float4>& a, int i, int c) -> double {
@@ -678,22 +703,27 @@ struct Impl : EngineBase {
     }
 
     int profile(int iters, float* avg_ms) override {
-        std::vector<cudaEvent_t> ev(2 * iters);
+        // groups of kProfileBurst launches back to back between two events;
+        // the device-gated rebuild runs after each group
+        constexpr int kProfileBurst = 4;
+        const int groups = (iters + kProfileBurst - 1) / kProfileBurst;
+        std::vector<cudaEvent_t> ev(2 * groups);
         for (auto& e : ev) CKE(cudaEventCreate(&e));
-        for (int q = 0; q < iters; q++) {
+        for (int q = 0; q < groups; q++) {
             CKE(cudaEventRecord(ev[2 * q], st));
-            launch_step(v, st, 0, 0);
+            for (int b = 0; b < kProfileBurst; b++) launch_step(v, st, 0, 0);
             CKE(cudaEventRecord(ev[2 * q + 1], st));
             launch_rebuild(v, st, /*force=*/0);
         }
         CKE(cudaStreamSynchronize(st));
         CKE(cudaGetLastError());
         double tot = 0.;
-        for (int q = 0; q < iters; q++) {
+        for (int q = 0; q < groups; q++) {
             float ms = 0.f;
             CKE(cudaEventElapsedTime(&ms, ev[2 * q], ev[2 * q + 1]));
             tot += ms;
         }
+        iters = groups * kProfileBurst;
         for (auto& e : ev) cudaEventDestroy(e);
         *avg_ms = (float)(tot / iters);
         return GDEM_OK;

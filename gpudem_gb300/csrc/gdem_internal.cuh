@@ -85,13 +85,14 @@ struct Ctl {
 
 template <class T>
 struct SBank {
-    double4_32a* pos;
+    double4_32a* pos;        // FP64 mode: {x, y, z, r}
     typename T::v4* vel;
     typename T::v4* rot;
-    // mixed mode only: the positions as unevaluated float pairs x = hi + lo
-    // (hi = fl32(x), lo = fl32(x - hi)), which neighbours gather instead of
-    // pos, so a pair's relative vector is formed at FP64 accuracy with FP32
-    // adds: posh = {hi.xyz, r}, posl = {lo.xyz, status}
+    // mixed mode: the positions as unevaluated float pairs x = hi + lo
+    // (|lo| <= ulp(hi)/2, about 48 significant bits), the only copy of the
+    // positions: posh = {hi.xyz, r}, posl = {lo.xyz, status}.  A pair's
+    // relative vector (hi_i - hi_j) + (lo_i - lo_j) is formed at FP64
+    // accuracy with FP32 adds, and hi + lo is exact in FP64.
     float4* posh;
     float4* posl;
     // mixed mode: low parts of the velocity and spin float pairs {lo.xyz, 0}
@@ -138,8 +139,9 @@ struct View {
     Ctl* ctl;
     // lists (rebuilt, not reordered)
     int *nei, *nnei, *neiw, *nneiw;
-    double4_32a* ref;                    // {x, y, z, -} at the last rebuild
-    float4 *refh, *refl;             // mixed mode: the same as float pairs
+    double4_32a* ref;                // FP64 mode: {x, y, z, -} at the last rebuild
+    float4* refh;                    // mixed mode: {hi.xyz, -} at the last rebuild
+    float4* posf;                    // FP64 mode: FP32 positions for the list prefilter
     int nei_cap, wall_cap, hist_cap, histw_cap;
     // per-step force/torque output
     double *fx, *fy, *fz, *tx, *ty, *tz;
@@ -168,7 +170,24 @@ struct View {
     double invdx, invdy, invdz;
     double skin, thresh_sq;
     float boxf[6];                   // mixed mode: box rounded outwards to FP32
+    float nb_delta;                  // bound on |d_fp32 - d| of the list prefilter (m)
+    // the scalars above rounded to FP32 once, for the mixed step
+    float dtf, gxf, gyf, gzf, thresh_sqf;
+    float muf, kn_cf, sn_cf, kt_cf, damp_cf, mu_rollf;
 };
+
+// Position {x, y, z, r} of particle i in FP64: the master in FP64 mode, the
+// float pair hi + lo (exact in FP64) in mixed mode.
+template <class T>
+__device__ __forceinline__ double4_32a load_pos(const SBank<T>& S, int i) {
+    if constexpr (T::mixed) {
+        const float4 h = S.posh[i], l = S.posl[i];
+        return make_double4_32a((double)h.x + (double)l.x, (double)h.y + (double)l.y,
+                                (double)h.z + (double)l.z, (double)h.w);
+    } else {
+        return S.pos[i];
+    }
+}
 
 // ---------------------------------------------------------------- Morton
 // 10-bit spread and interleave (x -> bit 2, y -> bit 1, z -> bit 0), the
@@ -355,8 +374,14 @@ __device__ __forceinline__ void split2(double x, float& hi, float& lo) {
 // step kernels (gdem_step_fp64.cu, gdem_step_mixed.cu)
 void launch_step(const View<FP64>& v, cudaStream_t st, cudaGraphConditionalHandle cond, int use_cond);
 void launch_step(const View<Mixed>& v, cudaStream_t st, cudaGraphConditionalHandle cond, int use_cond);
-void* step_kernel(const View<FP64>& v);
-void* step_kernel(const View<Mixed>& v);
+// The step kernel a launch uses and its launch shape.
+struct StepLaunch {
+    void* fn;
+    dim3 grid, block;
+    size_t smem;
+};
+StepLaunch step_launch(const View<FP64>& v);
+StepLaunch step_launch(const View<Mixed>& v);
 // stats and probes (gdem_stats.cu)
 template <class T>
 void launch_stats(const View<T>& v, double* partials, int nblk, cudaStream_t st);

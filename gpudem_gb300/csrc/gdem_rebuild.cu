@@ -187,7 +187,7 @@ __global__ void k_keys(View<T> v, int gated) {
     const SBank<T> S = v.S[ctl->s];
     uint32_t key = kNoKey;
     if (S.rot[i].w != 0) {
-        const double4_32a p = S.pos[i];
+        const double4_32a p = load_pos(S, i);
         const int cx = cell_coord(p.x, v.minx, v.invdx);
         const int cy = cell_coord(p.y, v.miny, v.invdy);
         const int cz = cell_coord(p.z, v.minz, v.invdz);
@@ -228,7 +228,7 @@ __global__ void k_reorder(View<T> v, int gated) {
     if (i < n) {
         const int src = v.vals[0][i];
         const SBank<T> A = v.S[s], B = v.S[s ^ 1];
-        B.pos[i] = A.pos[src];
+        if (!T::mixed) B.pos[i] = A.pos[src];
         B.vel[i] = A.vel[src];
         B.rot[i] = A.rot[src];
         if (T::mixed) {
@@ -322,11 +322,29 @@ __global__ void k_cell_ranges(View<T> v, int gated) {
 }
 
 // ===================================================================== Verlet lists
+// FP64 mode: FP32 copy of the positions for the prefilter of k_neighbors.
+template <class T>
+__global__ void k_posf(View<T> v, int gated) {
+    const Ctl* ctl = v.ctl;
+    if (gated && ctl->refresh == 0u) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.n) return;
+    const double4_32a p = v.S[ctl->s].pos[i];
+    v.posf[i] = make_float4((float)p.x, (float)p.y, (float)p.z, (float)p.w);
+}
+
 // One thread per particle: scan the 27 cells around its cell, keep every
 // listed j != i with |xi - xj|^2 < (ri + rj + skin)^2 (the test of
 // BoundingBox.cu:1136-1144, FP64 in every mode), order the row by the
 // partner's pId (the reference's index space) and record the reference
 // position.  Cells outside the grid hold nobody and are skipped.
+//
+// Most candidates are far from the cutoff, so each is first tested on FP32
+// positions: nb_delta bounds how far the FP32 distance can be from the FP64
+// one (eight FP32 ulps of the largest box coordinate, more than the two
+// roundings of the coordinates), and only a candidate whose FP32 distance is
+// within that band of the cutoff takes the FP64 test.  The decision is the
+// FP64 test's in every case.
 template <class T, int CAP>
 __global__ void __launch_bounds__(kBlock) k_neighbors(View<T> v, int gated) {
     Ctl* ctl = v.ctl;
@@ -336,14 +354,17 @@ __global__ void __launch_bounds__(kBlock) k_neighbors(View<T> v, int gated) {
     const int s = ctl->s, p = ctl->p;
     const SBank<T> S = v.S[s];
     const PBank<T> P = v.P[p];
+    const float4* __restrict__ PF = T::mixed ? S.posh : v.posf;
     int count = 0;
     if (i < n) {
         if (S.rot[i].w == 0) {
             v.nnei[i] = 0;
         } else {
-            const double4_32a pi = S.pos[i];
+            const double4_32a pi = load_pos(S, i);
+            const float4 fi = PF[i];
             const double xi = pi.x, yi = pi.y, zi = pi.z, ri = pi.w;
             const double skin = v.skin;
+            const float skinf = (float)v.skin, delta = v.nb_delta;
             const int cx = cell_coord(xi, v.minx, v.invdx);
             const int cy = cell_coord(yi, v.miny, v.invdy);
             const int cz = cell_coord(zi, v.minz, v.invdz);
@@ -364,13 +385,23 @@ __global__ void __launch_bounds__(kBlock) k_neighbors(View<T> v, int gated) {
                         for (int q = b; q < e; q++) {
                             const int j = v.reorder ? q : v.vals[0][q];
                             if (j == i) continue;
-                            const double4_32a pj = S.pos[j];
-                            const double dx = xi - pj.x;
-                            const double dy = yi - pj.y;
-                            const double dz = zi - pj.z;
-                            const double distsq = dx * dx + dy * dy + dz * dz;
-                            const double R = ri + pj.w + skin;
-                            if (distsq < R * R) {
+                            const float4 fj = PF[j];
+                            const float ex = fi.x - fj.x, ey = fi.y - fj.y, ez = fi.z - fj.z;
+                            const float dsqf = ex * ex + ey * ey + ez * ez;
+                            const float Rf = fi.w + fj.w + skinf;
+                            const float Rhi = Rf + delta, Rlo = Rf - delta;
+                            if (dsqf > Rhi * Rhi * 1.0000039f) continue;  // (1 + 2^-18): surely outside
+                            bool inside = Rlo > 0.f && dsqf < Rlo * Rlo * 0.9999962f;  // surely inside
+                            if (!inside) {
+                                const double4_32a pj = load_pos(S, j);
+                                const double dx = xi - pj.x;
+                                const double dy = yi - pj.y;
+                                const double dz = zi - pj.z;
+                                const double distsq = dx * dx + dy * dy + dz * dz;
+                                const double R = ri + pj.w + skin;
+                                inside = distsq < R * R;
+                            }
+                            if (inside) {
                                 const int pid_j = P.pid[j];
                                 if (count >= CAP) {
                                     overflow = true;
@@ -395,21 +426,10 @@ __global__ void __launch_bounds__(kBlock) k_neighbors(View<T> v, int gated) {
             const int m = count < v.nei_cap ? count : v.nei_cap;
             for (int k = 0; k < m; k++) v.nei[(size_t)k * n + i] = cand_j[k];
             v.nnei[i] = m;
-            v.ref[i] = make_double4_32a(xi, yi, zi, 0.0);
-            if (T::mixed) {
-                // reference position and a fresh float-pair split of the master
-                float4 h, l;
-                split2(xi, h.x, l.x);
-                split2(yi, h.y, l.y);
-                split2(zi, h.z, l.z);
-                h.w = l.w = 0.f;
-                v.refh[i] = h;
-                v.refl[i] = l;
-                h.w = (float)ri;
-                l.w = (float)S.rot[i].w;
-                S.posh[i] = h;
-                S.posl[i] = l;
-            }
+            if (T::mixed)
+                v.refh[i] = make_float4(fi.x, fi.y, fi.z, 0.f);
+            else
+                v.ref[i] = make_double4_32a(xi, yi, zi, 0.0);
         }
     }
     int wmax = count;
@@ -438,7 +458,7 @@ __global__ void __launch_bounds__(kBlock) k_wall_lists(View<T> v, int gated) {
         if (S.rot[i].w == 0 || v.ntri == 0) {
             v.nneiw[i] = 0;
         } else {
-            const double4_32a pi = S.pos[i];
+            const double4_32a pi = load_pos(S, i);
             const double px = pi.x, py = pi.y, pz = pi.z;
             const double R = pi.w + v.skin;
             const double Rsq = R * R;
@@ -517,6 +537,7 @@ void launch_rebuild(const View<T>& v, cudaStream_t st, int force) {
     const int gc = grid_for(v.ncells) < 4096 ? grid_for(v.ncells) : 4096;
     k_cells_clear<T><<<gc, kBlock, 0, st>>>(v, gated);
     k_cell_ranges<T><<<g, kBlock, 0, st>>>(v, gated);
+    if constexpr (!T::mixed) k_posf<T><<<g, kBlock, 0, st>>>(v, gated);
     if (v.nei_cap <= 32)
         k_neighbors<T, 32><<<g, kBlock, 0, st>>>(v, gated);
     else if (v.nei_cap <= 64)

@@ -32,7 +32,7 @@ __global__ void __launch_bounds__(kBlock) k_stats(View<T> v, double* partials) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const auto w = S.rot[i];
         if (w.w != 1) continue;
-        const double4_32a p = S.pos[i];
+        const double4_32a p = load_pos(S, i);
         const auto ve = S.vel[i];
         const double r = p.w;
         const double m = 1. / (double)ve.w, I = 1. / (double)P.mat[i].w;
@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(kBlock) k_stats(View<T> v, double* partials) {
         for (int k = 0; k < nn; k++) {
             const int j = v.nei[(size_t)k * n + i];
             if (S.rot[j].w != 1) continue;
-            const double4_32a q = S.pos[j];
+            const double4_32a q = load_pos(S, j);
             const double dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
             const double R = r + q.w;
             const double d2 = dx * dx + dy * dy + dz * dz;
@@ -90,7 +90,7 @@ __global__ void k_keys_probe(View<T> v, uint32_t* out) {
     const SBank<T> S = v.S[v.ctl->s];
     uint32_t key = kNoKey;
     if (S.rot[i].w == 1) {
-        const double4_32a p = S.pos[i];
+        const double4_32a p = load_pos(S, i);
         const int cx = cell_coord(p.x, v.minx, v.invdx);
         const int cy = cell_coord(p.y, v.miny, v.invdy);
         const int cz = cell_coord(p.z, v.minz, v.invdz);
@@ -109,7 +109,7 @@ template <class T>
 __global__ void k_gather_positions(View<T> v, double* out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.n) return;
-    const double4_32a p = v.S[v.ctl->s].pos[i];
+    const double4_32a p = load_pos(v.S[v.ctl->s], i);
     const int q = v.P[v.ctl->p].pid[i];
     out[3 * (size_t)q + 0] = p.x;
     out[3 * (size_t)q + 1] = p.y;

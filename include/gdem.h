@@ -42,6 +42,7 @@ extern "C" {
 #define GDEM_EW_BVH_STACK 0x10u      /* BVH traversal stack exhausted */
 #define GDEM_EW_NONFINITE 0x20u      /* NaN or Inf in a position or velocity */
 #define GDEM_EW_CELL_RANGE 0x40u     /* active particle outside the cell grid */
+#define GDEM_EW_TIMEOUT 0x80u        /* a bounded wait for a bulk copy gave up (results invalid) */
 
 /* ---- modes ---- */
 #define GDEM_FP64 0           /* plain FP64, bit-compatible with the reference CPU path */
@@ -246,10 +247,12 @@ int gdem_export_mesh(gdem_handle* h, double* rec, int* irec, double* aabb, uint3
  * recording timing events around gdem_step. */
 int gdem_get_stream(gdem_handle* h, void** stream);
 
-/* Time the step kernel alone: `iters` launches, each bracketed by CUDA events
- * on the handle's stream and followed by the (device-gated) list rebuild, so
- * the state stays valid.  avg_ms receives the mean step-kernel duration.
- * Advances the simulation by `iters` steps. */
+/* Time the step kernel alone: `iters` launches (rounded up to a multiple of
+ * 4) in groups of 4 back to back, each group bracketed by CUDA events on the
+ * handle's stream and followed by the device-gated list rebuild.  A rebuild
+ * that a step requests therefore runs up to 3 steps late: the lists stay
+ * valid while no particle moves more than skin/2 in 3 steps.  avg_ms receives
+ * the mean step-kernel duration.  Advances the simulation by the launches. */
 int gdem_profile_step(gdem_handle* h, int iters, float* avg_ms);
 
 #ifdef __cplusplus
