@@ -2,8 +2,12 @@
 
 Workload (the configuration the headline metric is quoted on): 1,000,000
 spheres with lognormal radii (median 1 mm, sigma_log 0.15, clipped to
-[0.6, 1.6] mm) over a seeded parametric helical chute (radius 0.3 m, pitch
-0.1 m, ~50,000 triangles), dt = 1e-6 s.  Synthetic, seeded inputs; no dataset.
+[0.6, 1.6] mm) poured into a seeded parametric helical chute (radius 0.3 m,
+pitch 0.1 m, 3 turns, ~50,000 triangles), Hertz-Mindlin, dt = 1e-6 s, 2,000
+timed steps.  The pour itself (a loose lattice above every turn, settled on
+the GPU with a larger time step before timing) is part of the setup, not of
+the timed region; the timed steps run on the resulting dense bed (about 4.6
+contacts per sphere).  Synthetic, seeded inputs; no dataset.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference]
 
@@ -131,15 +135,27 @@ def _time_steps(E, steps, warmup, stream, clk=None):
     return start.elapsed_time(stop), st0, st1
 
 
+def workload(args):
+    """The benchmark scene: the poured chute bed (default) or the loose
+    lattice over the chute with random velocities (`--workload lattice`)."""
+    from gpudem_gb300 import scenes
+    if args.workload == "lattice":
+        return scenes.config3_helical_chute(n=args.n, n_tri=args.ntri, v_sigma=args.v_sigma), 0.0
+    t0 = time.time()
+    sc = scenes.settle_scene(scenes.config3_chute_pour(n=args.n, n_tri=args.ntri), steps=args.settle_steps)
+    return sc, time.time() - t0
+
+
 def run_engine(args):
     import torch
     from gpudem_gb300 import engine, scenes
     dist, rank, ws = dist_init()
     lrank = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(lrank)
-    sc = scenes.config3_helical_chute(n=args.n, n_tri=args.ntri, v_sigma=args.v_sigma)
+    sc, pour_s = workload(args)
     kw = dict(model=args.model, reorder=True, nei_capacity=args.nei_cap, steps_per_graph=8,
-              skin=args.skin if args.skin > 0 else None)
+              skin=args.skin if args.skin > 0 else None, hist_capacity=32,
+              bvh_every_step=not args.bvh_once)
     t0 = time.time()
     E = engine.Engine(sc, precision=args.precision, **kw)
     setup_s = time.time() - t0
@@ -165,6 +181,12 @@ def run_engine(args):
     reb = int(st1["rebuilds"] - st0["rebuilds"])
     E.close()
     extra = {}
+    if not args.bvh_once:
+        # context: the same steps with the LBVH of the static mesh built once
+        E1 = engine.Engine(sc, precision=args.precision, **dict(kw, bvh_every_step=False))
+        ms1, a0, a1 = _time_steps(E1, max(10, args.steps // 4), args.warmup, torch.cuda.ExternalStream(E1.stream()))
+        E1.close()
+        extra["value_lbvh_built_once"] = 0.5 * (a0["n_active"] + a1["n_active"]) * max(10, args.steps // 4) / (ms1 / 1e3)
     if mixed and not args.no_fp64:
         # the same engine in plain FP64 on the same workload (the ratio's denominator)
         F = engine.Engine(sc, precision="fp64", **kw)
@@ -173,7 +195,7 @@ def run_engine(args):
         fms, f0, f1 = _time_steps(F, fsteps, args.warmup, fstream)
         fval = 0.5 * (f0["n_active"] + f1["n_active"]) * fsteps / (fms / 1e3)
         F.close()
-        extra = {"fp64_value": fval, "fp64_steps": fsteps, "mixed_over_fp64": value / fval}
+        extra.update({"fp64_value": fval, "fp64_steps": fsteps, "mixed_over_fp64": value / fval})
         if args.error_steps > 0:
             extra.update(position_error(sc, kw, args.error_steps))
     # end to end through the C ABI with host buffers
@@ -182,19 +204,29 @@ def run_engine(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32+f64" if mixed else "f64",
-        "data": "synthetic (seeded lognormal spheres on a lattice over a generated helical chute)",
-        "config": {"workload": f"helical chute, {args.n} lognormal spheres (median 1 mm, sigma_log 0.15), "
-                               f"{sc.tris.shape[0]} triangles, dt=1e-6 s, {args.model}, {args.precision}",
+        "dtype": "f32" if mixed else "f64",
+        "data": ("synthetic (seeded lognormal spheres poured into a generated helical chute, settled on the GPU "
+                 "before timing)" if args.workload == "poured" else
+                 "synthetic (seeded lognormal spheres on a lattice over a generated helical chute)"),
+        "config": {"workload": (f"helical chute, {args.n} lognormal spheres (median 1 mm, sigma_log 0.15), "
+                                f"{sc.tris.shape[0]} triangles, dt=1e-6 s, {args.model}, {args.precision}, "
+                                + (f"poured bed (settled {args.settle_steps} steps at dt=2e-5 s, e=0.1)"
+                                   if args.workload == "poured" else "loose lattice, v_sigma "
+                                   f"{args.v_sigma} m/s")),
                    "n_particles": args.n, "n_triangles": int(sc.tris.shape[0]), "precision": args.precision,
                    "model": args.model, "l2": "inputs larger than L2 (state + lists > 129 MB per step)",
                    "parallelism": "replicas" if ws > 1 else "single GPU",
-                   "rebuilds_in_timed_region": reb, "setup_s": round(setup_s, 2), **extra},
+                   "lbvh": "built once (static mesh)" if args.bvh_once else "rebuilt every step",
+                   "rebuilds_in_timed_region": reb, "setup_s": round(setup_s, 2), "pour_s": round(pour_s, 1),
+                   "contacts_per_sphere": round(stk["n_contacts"] / max(stk["n_active"], 1), 3),
+                   "wall_contacts_per_sphere": round(stk["n_wall_contacts"] / max(stk["n_active"], 1), 3),
+                   **extra},
         "clocks": clk.summary(),
-        # one step kernel per step + the rebuild kernels of each rebuild
-        # (keys, 4 x 3 sort passes, reorder, cell clear, cell ranges, Verlet, walls)
-        # (+ the FP32 position copy of the FP64 mode's list prefilter)
-        "gpu_launches": args.steps + reb * (18 if mixed else 19),
+        # one step kernel per step (+ the LBVH rebuild: keys, 4 x 3 sort passes,
+        # init, internal nodes, refit) + the kernels of each list rebuild (keys,
+        # 4 x 3 sort passes, reorder (+ its inverse order in mixed mode), cell
+        # clear, cell ranges, Verlet (+ the FP32 position copy in FP64 mode), walls)
+        "gpu_launches": args.steps * (1 + (0 if args.bvh_once else 16)) + reb * 19,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": args.traffic,
                      "peak_kind": f"{peak_kind} hbm_gbs",
@@ -241,16 +273,30 @@ def run_e2e(args, sc, kw):
     frame = torch.empty(3 * n, dtype=torch.float64).pin_memory().numpy()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    E.import_particles(sc)
+    E.import_particles(sc, history=sc.history, hist_stride=sc.hist_stride)
     for _ in range(steps):
         E.step(1)
         E.export_positions(out=frame)
     E.sync()
     dt_s = time.perf_counter() - t0
     E.close()
-    h2d = n * (4 * 8 * 3 + 4 * 8)
+    h2d = n * (3 * 8 * 3 + 4 * 8 + 4)
+    if sc.history is not None:
+        h2d += sum(int(np.asarray(a).nbytes) for a in sc.history.values())
     return {"value": n * steps / dt_s, "unit": UNIT, "h2d_bytes_per_step": h2d / steps,
             "d2h_bytes_per_step": frame.nbytes, "steps": steps}
+
+
+def active_only(sc):
+    """The scene without the spheres that have left the box (frozen, never a
+    contact partner again), for the CPU path, which takes no activity flags."""
+    from dataclasses import replace
+    if sc.active is None or bool(np.all(sc.active)):
+        return sc
+    a = np.asarray(sc.active, bool)
+    pick = lambda x: None if x is None else np.asarray(x)[a]
+    return replace(sc, x=sc.x[a], r=sc.r[a], m=sc.m[a], k=sc.k[a], eta=sc.eta[a], v=pick(sc.v), w=pick(sc.w),
+                   history=None, hist_stride=0, active=None)
 
 
 def cpu_baseline(args, sc):
@@ -261,26 +307,27 @@ def cpu_baseline(args, sc):
     except Exception as e:  # noqa: BLE001
         return {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                 "sample": f"unavailable: {e}"}
-    return port.time_sample(sc, budget_s=args.cpu_budget)
+    return port.time_sample(active_only(sc), budget_s=args.cpu_budget)
 
 
 def run_reference(args):
     dist, rank, ws = dist_init()
     if rank != 0:
         return
-    from gpudem_gb300 import scenes
-    sc = scenes.config3_helical_chute(n=args.n, n_tri=args.ntri, v_sigma=args.v_sigma)
+    # the same bed as the engine arm: poured (settled) by the engine on the GPU
+    # as input preparation; the timed steps run the CPU path only
+    sc, _ = workload(args)
     try:
         from oracle import port
-        res = port.time_steps(sc, steps=args.steps, warmup=args.warmup, budget_s=args.cpu_budget)
+        res = port.time_steps(active_only(sc), steps=args.steps, warmup=args.warmup, budget_s=args.cpu_budget)
     except Exception as e:  # noqa: BLE001
         print(json.dumps({"impl": "reference", "unavailable": f"oracle port failed: {e}"}))
         return
     out = {"impl": "reference", "metric": METRIC, "value": res["value"], "unit": UNIT, "n_gpus": ws,
            "steps": res["steps"], "warmup": args.warmup, "ms_per_step": res["ms_per_step"],
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-           "data": "synthetic", "config": {"workload": f"helical chute, {args.n} lognormal spheres, "
-                                                       f"reference CPU path (linear model), sample"},
+           "data": "synthetic", "config": {"workload": f"helical chute, {args.n} lognormal spheres, {args.workload} "
+                                                       f"bed, reference CPU path (linear model), sample"},
            "cpu_baseline": {"value": res["value"], "unit": UNIT, "cores": res["cores"], "kind": "port",
                             "sample": res["sample"]},
            "e2e": {"value": res["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -290,7 +337,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=40)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--n", type=int, default=1_000_000)
@@ -306,7 +353,11 @@ def main():
     ap.add_argument("--skin", type=float, default=-1.0)
     ap.add_argument("--v-sigma", type=float, default=0.5)
     ap.add_argument("--profile-iters", type=int, default=10)
-    ap.add_argument("--e2e-steps", type=int, default=50)
+    ap.add_argument("--e2e-steps", type=int, default=500)
+    ap.add_argument("--workload", default="poured", choices=["poured", "lattice"])
+    ap.add_argument("--bvh-once", action="store_true",
+                    help="build the static mesh's LBVH once instead of in every step")
+    ap.add_argument("--settle-steps", type=int, default=12000)
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()

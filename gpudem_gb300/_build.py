@@ -34,6 +34,9 @@ UNITS = {
     "gdem_stats.cu": True,
     "gdem_noalloc.cu": True,
 }
+# the mixed-precision step: FP32 contact law with the hardware's approximate
+# reciprocal and square root (its error is measured against the FP64 mode)
+EXTRA = {"gdem_step_mixed.cu": ["-prec-div=false", "-prec-sqrt=false"]}
 
 
 def _nvcc():
@@ -67,7 +70,8 @@ def build_engine(verbose=False, ptxas_info=False) -> str:
         obj = os.path.join(OUT, unit.replace(".cu", ".o"))
         objs.append(obj)
         if _stale(obj, [src, *headers, __file__]):
-            cmd = [nvcc, *ARCH, *COMMON, "-fmad=false" if nofma else "-fmad=true", "-c", src, "-o", obj]
+            cmd = [nvcc, *ARCH, *COMMON, "-fmad=false" if nofma else "-fmad=true", *EXTRA.get(unit, []), "-c", src,
+                   "-o", obj]
             if ptxas_info:
                 cmd += ["-Xptxas", "-v"]
             jobs.append(cmd)

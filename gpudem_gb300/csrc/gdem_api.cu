@@ -54,8 +54,21 @@ struct MeshData {
     double* aabb_d = nullptr;
     uint32_t* morton[2] = {nullptr, nullptr};
     int* idx[2] = {nullptr, nullptr};
+    uint32_t *hist = nullptr, *tot = nullptr;  // key-sort scratch
+    int* flags = nullptr;                      // refit flags
+    double gmin[3] = {0., 0., 0.}, ginv[3] = {0., 0., 0.};
     std::vector<double> aabb_h;
 };
+
+// Rebuild the LBVH of a mesh already set: centroid keys, their stable sort,
+// internal nodes and boxes (the set-up's own steps).
+static void launch_bvh_rebuild(const MeshData& M, cudaStream_t st) {
+    if (M.ntri <= 0) return;
+    launch_tri_keys(M.rec, M.morton[0], M.idx[0], M.ntri, M.gmin, M.ginv, st);
+    radix_sort_pairs(M.morton[0], M.idx[0], M.morton[1], M.idx[1], M.hist, M.tot, M.ntri, rs_blocks_for(M.ntri), 0,
+                     4, st);
+    launch_bvh_build(M.aabb_d, M.nodes, M.morton[0], M.idx[0], M.flags, M.ntri, st);
+}
 
 // Everything that depends on the precision mode.
 struct EngineBase {
@@ -178,6 +191,7 @@ struct Impl : EngineBase {
             A.add(&v.tx, n); A.add(&v.ty, n); A.add(&v.tz, n);
             A.add(&v.ftmp, (size_t)6 * n);
         }
+        if (T::mixed) A.add(&v.inv, n);
         A.add(&v.rs_hist, (size_t)256 * v.rs_blocks);
         A.add(&v.rs_tot, 256);
         A.add(&v.ctl, 1);
@@ -233,8 +247,11 @@ struct Impl : EngineBase {
 
     TriRecF* trif = nullptr;
 
+    const MeshData* mesh = nullptr;
+
     void set_mesh(const MeshData& M) override {
         destroy_graphs();
+        mesh = &M;
         v.ntri = M.ntri;
         v.tri = M.rec;
         v.bvh = M.nodes;
@@ -268,6 +285,16 @@ struct Impl : EngineBase {
             kp.kernelParams = args;
             cudaGraphNode_t sn;
             CKE(cudaGraphAddKernelNode(&sn, g, prev ? &prev : nullptr, prev ? 1 : 0, &kp));
+            if (d.bvh_every_step && mesh && mesh->ntri > 0) {
+                cudaGraph_t bg;
+                CKE(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+                launch_bvh_rebuild(*mesh, st);
+                CKE(cudaStreamEndCapture(st, &bg));
+                cudaGraphNode_t bn;
+                CKE(cudaGraphAddChildGraphNode(&bn, g, &sn, 1, bg));
+                cudaGraphDestroy(bg);
+                sn = bn;
+            }
             cudaGraphNodeParams cp = {};
             cp.type = cudaGraphNodeTypeConditional;
             cp.conditional.handle = hnd;
@@ -457,6 +484,7 @@ struct Impl : EngineBase {
             // plain launches: step kernel, then the device-gated rebuild
             for (int q = 0; q < nsteps; q++) {
                 launch_step(v, st, 0, 0);
+                if (d.bvh_every_step && mesh) launch_bvh_rebuild(*mesh, st);
                 launch_rebuild(v, st, /*force=*/0);
             }
             CKE(cudaGetLastError());
@@ -564,7 +592,8 @@ struct Impl : EngineBase {
                 cnt[q] = nc[i];
                 for (int s2 = 0; s2 < nc[i] && s2 < stv; s2++) {
                     const size_t src = (size_t)s2 * n + i, dst = (size_t)q * stv + s2;
-                    if (ind) ind[dst] = id[src];
+                    // mixed-mode particle keys are storage indices: report pIds
+                    if (ind) ind[dst] = (T::mixed && did == P.hid) ? pid[id[src]] : id[src];
                     if (X) X[dst] = hx[src];
                     if (Y) Y[dst] = hy[src];
                     if (Z) Z[dst] = hz[src];
@@ -945,8 +974,7 @@ static int upload_mesh(gdem_handle* h, const std::vector<double>& vx, const std:
     const int NV = (int)vx.size();
     Arena A;
     double *dvx, *dvy, *dvz, *draw3;
-    int *dtv, *dte, *flags;
-    uint32_t *hist, *tot;
+    int *dtv, *dte;
     const int nb = rs_blocks_for(T);
     A.add(&M.rec, T);
     A.add(&M.nodes, 2 * (size_t)T);
@@ -954,11 +982,11 @@ static int upload_mesh(gdem_handle* h, const std::vector<double>& vx, const std:
     A.add(&dvx, NV); A.add(&dvy, NV); A.add(&dvz, NV);
     A.add(&draw3, raw3_h ? 3 * (size_t)T : (size_t)T);
     A.add(&dtv, 3 * (size_t)T); A.add(&dte, 3 * (size_t)T);
-    A.add(&flags, T);
+    A.add(&M.flags, T);
     A.add(&M.morton[0], T); A.add(&M.morton[1], T);
     A.add(&M.idx[0], T); A.add(&M.idx[1], T);
-    A.add(&hist, (size_t)256 * nb);
-    A.add(&tot, 256);
+    A.add(&M.hist, (size_t)256 * nb);
+    A.add(&M.tot, 256);
     CK(cudaMalloc((void**)&M.arena, A.total()));
     A.bind(M.arena);
     M.ntri = T;
@@ -975,8 +1003,12 @@ static int upload_mesh(gdem_handle* h, const std::vector<double>& vx, const std:
     launch_tri_precompute(M.rec, M.morton[0], M.idx[0], dvx, dvy, dvz, dtv, dte, raw3_h ? draw3 : nullptr,
                           raw3_h ? nullptr : draw3, T, g, inv, st);
     // stable sort of the centroid keys (radixSortUint32 at TriangleMesh.cu:722)
-    radix_sort_pairs(M.morton[0], M.idx[0], M.morton[1], M.idx[1], hist, tot, T, nb, 0, 4, st);
-    launch_bvh_build(M.aabb_d, M.nodes, M.morton[0], M.idx[0], flags, T, st);
+    for (int k = 0; k < 3; k++) {
+        M.gmin[k] = g[k];
+        M.ginv[k] = inv[k];
+    }
+    radix_sort_pairs(M.morton[0], M.idx[0], M.morton[1], M.idx[1], M.hist, M.tot, T, nb, 0, 4, st);
+    launch_bvh_build(M.aabb_d, M.nodes, M.morton[0], M.idx[0], M.flags, T, st);
     CK(cudaStreamSynchronize(st));
     CK(cudaGetLastError());
     h->eng->set_mesh(M);

@@ -80,7 +80,7 @@ struct Ctl {
     unsigned long long rebuilds;
     int max_nei, max_wall;
     int lists_valid;
-    int pad;
+    unsigned work;            // next sub-tile of the persistent step kernel (0 between steps)
 };
 
 template <class T>
@@ -107,7 +107,8 @@ struct PBank {
     typename T::v4* mat;
     int* pid;
     int* nc;                         // particle contacts in history
-    int* hid;                        // [hcap * n] pId of the contact partner
+    int* hid;                        // [hcap * n] contact partner: its pId (FP64 mode), its storage
+                                     // index (mixed mode; remapped when the particles are reordered)
     typename T::real *hx, *hy, *hz;  // [hcap * n] tangential spring
     typename T::real *cx, *cy, *cz;  // [hcap * n] compensation terms (mixed mode)
     int* ncw;                        // wall contacts in history
@@ -150,6 +151,7 @@ struct View {
     // sort scratch (ping-pong) and cell list
     uint32_t* keys[2];
     int* vals[2];
+    int* inv;                        // mixed mode: old storage index -> new, at a reorder
     uint32_t* rs_hist;               // [256 * rs_blocks]
     uint32_t* rs_tot;                // [256]
     int rs_blocks;
@@ -353,6 +355,10 @@ template <class T>
 void launch_rebuild(const View<T>& v, cudaStream_t st, int force);
 template <class T>
 void launch_finalize_oob(const View<T>& v, cudaStream_t st);
+// Triangle centroid Morton keys (and identity payload) from the records, as
+// k_tri_precompute computes them.
+void launch_tri_keys(const TriRec* rec, uint32_t* morton, int* idx, int ntri, const double* gmin,
+                     const double* invrange, cudaStream_t st);
 void launch_bvh_build(const double* aabb, BNode* nodes, const uint32_t* morton_sorted,
                       const int* sorted_idx, int* flags, int ntri, cudaStream_t st);
 void launch_tri_precompute(TriRec* rec, uint32_t* morton, int* idx, const double* vx,

@@ -216,6 +216,17 @@ void launch_finalize_oob(const View<T>& v, cudaStream_t st) {
 }
 
 // ===================================================================== reorder
+// Mixed mode: the inverse of the sort permutation, for remapping the history
+// keys (storage indices of contact partners) when the particles move.
+template <class T>
+__global__ void k_inverse_order(View<T> v, int gated) {
+    const Ctl* ctl = v.ctl;
+    if (gated && ctl->refresh == 0u) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.n) return;
+    v.inv[v.vals[0][i]] = i;
+}
+
 // Gather every per-particle array into sorted order (d_swap_ps,
 // BoundingBox.cu:928-1005, but with compact histories: only live slots move).
 template <class T>
@@ -244,7 +255,8 @@ __global__ void k_reorder(View<T> v, int gated) {
         Q.nc[i] = nc;
         for (int k = 0; k < nc; k++) {
             const size_t a = (size_t)k * n + src, b = (size_t)k * n + i;
-            Q.hid[b] = P.hid[a]; Q.hx[b] = P.hx[a]; Q.hy[b] = P.hy[a]; Q.hz[b] = P.hz[a];
+            Q.hid[b] = T::mixed ? v.inv[P.hid[a]] : P.hid[a];
+            Q.hx[b] = P.hx[a]; Q.hy[b] = P.hy[a]; Q.hz[b] = P.hz[a];
             if (T::mixed) { Q.cx[b] = P.cx[a]; Q.cy[b] = P.cy[a]; Q.cz[b] = P.cz[a]; }
         }
         const int ncw = P.ncw[src];
@@ -532,6 +544,7 @@ void launch_rebuild(const View<T>& v, cudaStream_t st, int force) {
             k_reorder_forces<T><<<g, kBlock, 0, st>>>(v, gated);
             k_copy_forces<T><<<g, kBlock, 0, st>>>(v, gated);
         }
+        if constexpr (T::mixed) k_inverse_order<T><<<g, kBlock, 0, st>>>(v, gated);
         k_reorder<T><<<g, kBlock, 0, st>>>(v, gated);
     }
     const int gc = grid_for(v.ncells) < 4096 ? grid_for(v.ncells) : 4096;
@@ -632,6 +645,30 @@ void launch_tri_precompute(TriRec* rec, uint32_t* morton, int* idx, const double
     k_tri_precompute<<<grid_for(ntri), kBlock, 0, st>>>(rec, morton, idx, vx, vy, vz, tv, te, raw3, dplane,
                                                         ntri, gmin[0], gmin[1], gmin[2], invrange[0],
                                                         invrange[1], invrange[2]);
+}
+
+// Centroid keys of the triangles from their records (the key formula of
+// k_tri_precompute), for rebuilding the LBVH of a mesh already set.
+__global__ void k_tri_keys(const TriRec* rec, uint32_t* morton, int* idx, int ntri, double gminx, double gminy,
+                           double gminz, double irx, double iry, double irz) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntri) return;
+    const TriRec& R = rec[t];
+    const double cx = (R.v0[0] + R.v1[0] + R.v2[0]) / 3.0;
+    const double cy = (R.v0[1] + R.v1[1] + R.v2[1]) / 3.0;
+    const double cz = (R.v0[2] + R.v1[2] + R.v2[2]) / 3.0;
+    const uint32_t ix = (uint32_t)((cx - gminx) * irx);
+    const uint32_t iy = (uint32_t)((cy - gminy) * iry);
+    const uint32_t iz = (uint32_t)((cz - gminz) * irz);
+    morton[t] = morton3(ix, iy, iz);
+    idx[t] = t;
+}
+
+void launch_tri_keys(const TriRec* rec, uint32_t* morton, int* idx, int ntri, const double* gmin,
+                     const double* invrange, cudaStream_t st) {
+    if (ntri <= 0) return;
+    k_tri_keys<<<grid_for(ntri), kBlock, 0, st>>>(rec, morton, idx, ntri, gmin[0], gmin[1], gmin[2], invrange[0],
+                                                  invrange[1], invrange[2]);
 }
 
 // ---- Karras (2012) LBVH over the Morton-sorted triangles.  Keys that tie are

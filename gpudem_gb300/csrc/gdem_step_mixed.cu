@@ -17,7 +17,8 @@
 //    compensated (Kahan) sum;
 //  * the refresh test and the out-of-box test use the high parts;
 //  * no FP64 arithmetic at all: the scalars arrive pre-rounded to FP32.
-// Compiled with multiply-add contraction on.
+// Compiled with multiply-add contraction on, and with the hardware's
+// approximate reciprocal and square root (-prec-div=false -prec-sqrt=false).
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
@@ -122,6 +123,7 @@ __device__ __forceinline__ void step_epilogue(Ctl* ctl, int s, bool refresh, uns
     if (last_block(&ctl->done[0])) {
         if (threadIdx.x == 0) {
             ctl->done[0] = 0;
+            ctl->work = 0;
             ctl->s = s ^ 1;
             ctl->steps += 1ull;
             const unsigned r = atomicAdd(&ctl->refresh, 0u);
@@ -137,328 +139,388 @@ struct Own {
     int nn, nw, nc, ncw;
 };
 
-// One particle's step: contacts, history, integration, refresh and
-// out-of-box tests.  Writes bank s^1 and the history.
+// Per-particle contact constants.
+struct Mat {
+    float ki, etai, sqrtmi, invmoi;
+};
+
+template <int MODEL>
+__device__ __forceinline__ Mat own_material(const PBank<Mixed>& P, int i, float ri, float invmi) {
+    Mat m;
+    if (MODEL == 0) {
+        const float4 mi = __ldg(&P.mat[i]);
+        m.ki = mi.x; m.etai = mi.y; m.sqrtmi = mi.z; m.invmoi = mi.w;
+    } else {
+        m.ki = m.etai = m.sqrtmi = 0.f;
+        m.invmoi = 2.5f * invmi / (ri * ri);  // 1 / (2/5 m r^2)
+    }
+    return m;
+}
+
+struct Force6 {
+    float fx, fy, fz, mx, my, mz;
+};
+
+// Force and torque on i from one particle contact (calc_normal_force /
+// calc_tangential_force, cpu_dem.cu:953, :783, or the Hertz-Mindlin law),
+// with the spring history (sp, cp) of the contact updated in place.
+template <int MODEL>
+__device__ __forceinline__ Force6 pair_force(const View<Mixed>& v, float dx, float dy, float dz, float ri, float rj,
+                                             float4 vi, float4 wi, float4 vj, float4 wj, float invmi, const Mat& m,
+                                             Vec3<float>& sp, Vec3<float>& cp) {
+    using R = float;
+    const R distsq = dx * dx + dy * dy + dz * dz;
+    const R Rs = ri + rj;
+    const R dist = sqrtf(distsq);
+    const R inv = 1.f / dist;
+    const R delMag = Rs - dist;
+    const R nx = dx * inv, ny = dy * inv, nz = dz * inv;
+    const R vrx = vi.x - vj.x, vry = vi.y - vj.y, vrz = vi.z - vj.z;
+    const R vdn = vrx * nx + vry * ny + vrz * nz;
+    const R vnx = vdn * nx, vny = vdn * ny, vnz = vdn * nz;
+    R fnx, fny, fnz, kt, gt, Rstar = 0.f;
+    if (MODEL == 0) {
+        const R meff = 1.f / (invmi + vj.w);
+        const R eta = m.etai * sqrtf(meff);
+        const R fel = m.ki * delMag;
+        fnx = fel * nx - eta * vnx;
+        fny = fel * ny - eta * vny;
+        fnz = fel * nz - eta * vnz;
+        kt = m.ki;
+        gt = eta;
+    } else {
+        Rstar = ri * rj / Rs;
+        const R mstar = 1.f / (invmi + vj.w);
+        const R sqrtRd = sqrtf(Rstar * delMag);
+        const R fel = v.kn_cf * sqrtRd * delMag;
+        const R gn = v.damp_cf * sqrtf(v.sn_cf * sqrtRd * mstar);
+        const R fnm = fel - gn * vdn;
+        fnx = fnm * nx;
+        fny = fnm * ny;
+        fnz = fnm * nz;
+        kt = v.kt_cf * sqrtRd;
+        gt = v.damp_cf * sqrtf(kt * mstar);
+    }
+    const R ax_ = ri * wi.x + rj * wj.x;
+    const R ay_ = ri * wi.y + rj * wj.y;
+    const R az_ = ri * wi.z + rj * wj.z;
+    const R vtx = (vrx - vnx) + (ay_ * nz - az_ * ny);
+    const R vty = (vry - vny) + (az_ * nx - ax_ * nz);
+    const R vtz = (vrz - vnz) + (ax_ * ny - ay_ * nx);
+    Vec3<R> ft;
+    const R fnsq = fnx * fnx + fny * fny + fnz * fnz;
+    tangential<Mixed>(nx, ny, nz, fnsq, vtx, vty, vtz, gt, kt, v.muf, v.dtf, sp, cp, ft);
+    Force6 F;
+    F.fx = fnx + ft.x;
+    F.fy = fny + ft.y;
+    F.fz = fnz + ft.z;
+    F.mx = ri * (ny * ft.z - nz * ft.y);
+    F.my = ri * (nz * ft.x - nx * ft.z);
+    F.mz = ri * (nx * ft.y - ny * ft.x);
+    if (MODEL == 1 && v.mu_rollf > 0.f) {
+        const R rx = wi.x - wj.x, ry = wi.y - wj.y, rz = wi.z - wj.z;
+        const R wn2 = rx * rx + ry * ry + rz * rz;
+        if (wn2 > 0.f) {
+            const R tr = -v.mu_rollf * Rstar * sqrtf(fnsq) * rsqrtf(wn2);
+            F.mx += tr * rx;
+            F.my += tr * ry;
+            F.mz += tr * rz;
+        }
+    }
+    return F;
+}
+
+// Wall contacts of particle i from its wall list, in list order
+// (wall_collision_verlet, cpu_dem.cu:238), added to f and m.
+template <int MODEL, int WCAP>
+__device__ __forceinline__ void wall_forces(const View<Mixed>& v, const PBank<Mixed>& P, int i, int nw, int ncw,
+                                            float4 hi, float4 li, float4 vi, float4 wi, float invmi, const Mat& mt,
+                                            Force6& F, unsigned& err) {
+    using T = Mixed;
+    using R = float;
+    const int n = v.n;
+    const int* __restrict__ neiw = v.neiw;
+    const R ri = hi.w;
+    unsigned long long wtouched = 0ull;
+    int vore[WCAP];
+    int nvore = 0;
+    const float3 ph = make_float3(hi.x, hi.y, hi.z), pl = make_float3(li.x, li.y, li.z);
+    const R rsq = ri * ri;
+    for (int k0 = 0; k0 < nw; k0 += 4) {
+        // four candidates at a time: their indices, then the first 48 bytes
+        // of their records (corner pair and normal), all in flight together,
+        // for the plane-distance test that rejects most of them
+        int tt[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) tt[q] = k0 + q < nw ? __ldg(&neiw[(size_t)(k0 + q) * n + i]) : -1;
+        unsigned near = 0u;
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            if (tt[q] < 0) continue;
+            const float4* rec = reinterpret_cast<const float4*>(&v.trif[tt[q]]);
+            const float4 a = __ldg(rec), b = __ldg(rec + 1), c = __ldg(rec + 2);
+            // a = {v0h.xyz, v0l.x}, b = {v0l.yz, n.xy}, c = {n.z, ...}
+            const float ax = (ph.x - a.x) + (pl.x - a.w);
+            const float ay = (ph.y - a.y) + (pl.y - b.x);
+            const float az = (ph.z - a.z) + (pl.z - b.y);
+            const float dist = b.z * ax + b.w * ay + c.x * az;
+            if (!(dist * dist > rsq)) near |= 1u << q;
+        }
+        while (near) {
+            const int q = __ffs(near) - 1;
+            near &= near - 1u;
+            const int t = __ldg(&neiw[(size_t)(k0 + q) * n + i]);
+            const FeatureF f = closest_feature_f(ph, pl, rsq, v.trif[t]);
+            if (!(f.dist < ri)) continue;
+        if (f.hit != -1) {
+            bool dup = false;
+            for (int q = 0; q < nvore; q++)
+                if (vore[q] == f.hit) {
+                    dup = true;
+                    break;
+                }
+            if (dup) continue;
+            if (nvore < WCAP) vore[nvore++] = f.hit;
+        }
+        const R delmag = ri - f.dist;
+        const R nx = f.nx, ny = f.ny, nz = f.nz;
+        const R vdn = vi.x * nx + vi.y * ny + vi.z * nz;
+        const R vnx = vdn * nx, vny = vdn * ny, vnz = vdn * nz;
+        R fnx, fny, fnz, kt, gt;
+        if (MODEL == 0) {
+            const R eta = mt.etai * mt.sqrtmi;
+            const R fel = mt.ki * delmag;
+            fnx = fel * nx - eta * vnx;
+            fny = fel * ny - eta * vny;
+            fnz = fel * nz - eta * vnz;
+            kt = mt.ki;
+            gt = eta;
+        } else {
+            const R mstar = 1.f / invmi;
+            const R sqrtRd = sqrtf(ri * delmag);
+            const R fel = v.kn_cf * sqrtRd * delmag;
+            const R gn = v.damp_cf * sqrtf(v.sn_cf * sqrtRd * mstar);
+            const R fnm = fel - gn * vdn;
+            fnx = fnm * nx;
+            fny = fnm * ny;
+            fnz = fnm * nz;
+            kt = v.kt_cf * sqrtRd;
+            gt = v.damp_cf * sqrtf(kt * mstar);
+        }
+        const R ax_ = ri * wi.x, ay_ = ri * wi.y, az_ = ri * wi.z;
+        const R vtx = (vi.x - vnx) + (ay_ * nz - az_ * ny);
+        const R vty = (vi.y - vny) + (az_ * nx - ax_ * nz);
+        const R vtz = (vi.z - vnz) + (ax_ * ny - ay_ * nx);
+        F.fx += fnx;
+        F.fy += fny;
+        F.fz += fnz;
+        bool fresh;
+        const int slot = find_slot<T>(P.hwid, n, i, ncw, t, v.histw_cap, fresh);
+        if (slot < 0) {
+            err |= 0x8u;
+            continue;
+        }
+        const size_t h = (size_t)slot * n + i;
+        Vec3<R> sp, cp;
+        if (fresh) {
+            P.hwid[h] = t;
+            sp.x = sp.y = sp.z = 0.f;
+            cp.x = cp.y = cp.z = 0.f;
+        } else {
+            sp.x = P.hwx[h]; sp.y = P.hwy[h]; sp.z = P.hwz[h];
+            cp.x = P.cwx[h]; cp.y = P.cwy[h]; cp.z = P.cwz[h];
+        }
+        wtouched |= 1ull << slot;
+        Vec3<R> ft;
+        const R fnsq = fnx * fnx + fny * fny + fnz * fnz;
+        tangential<T>(nx, ny, nz, fnsq, vtx, vty, vtz, gt, kt, v.muf, v.dtf, sp, cp, ft);
+        F.fx += ft.x;
+        F.fy += ft.y;
+        F.fz += ft.z;
+        F.mx += ri * (ny * ft.z - nz * ft.y);
+        F.my += ri * (nz * ft.x - nx * ft.z);
+        F.mz += ri * (nx * ft.y - ny * ft.x);
+        if (MODEL == 1 && v.mu_rollf > 0.f) {
+            const R wn2 = wi.x * wi.x + wi.y * wi.y + wi.z * wi.z;
+            if (wn2 > 0.f) {
+                const R tr = -v.mu_rollf * ri * sqrtf(fnsq) * rsqrtf(wn2);
+                F.mx += tr * wi.x;
+                F.my += tr * wi.y;
+                F.mz += tr * wi.z;
+            }
+        }
+        P.hwx[h] = sp.x; P.hwy[h] = sp.y; P.hwz[h] = sp.z;
+        P.cwx[h] = cp.x; P.cwy[h] = cp.y; P.cwz[h] = cp.z;
+        }
+    }
+    P.ncw[i] = surviving(wtouched, ncw);
+}
+
+// Inactive particle, or one that left the box last step (status 2): frozen
+// from now on.
+__device__ __forceinline__ void freeze_one(const View<Mixed>& v, const SBank<Mixed>& B, int i, const Own& o) {
+    float4 li = o.li, wi = o.wi;
+    B.posh[i] = o.hi;
+    li.w = 0.f;
+    B.posl[i] = li;
+    B.vel[i] = o.vi;
+    B.vell[i] = o.vl;
+    B.rotl[i] = o.wl;
+    wi.w = 0.f;
+    B.rot[i] = wi;
+    if (v.store_forces) {
+        v.fx[i] = 0.; v.fy[i] = 0.; v.fz[i] = 0.;
+        v.tx[i] = 0.; v.ty[i] = 0.; v.tz[i] = 0.;
+    }
+}
+
+// Symplectic Euler (cpu_dem.cu:1622-1652) on the float pairs of position,
+// velocity and spin, so their many small increments do not round away; the
+// refresh and out-of-box tests; the new state into bank s^1.
+__device__ __forceinline__ void integrate_one(const View<Mixed>& v, const SBank<Mixed>& B, int i, const Own& o,
+                                              float invmoi, const Force6& F, bool& refresh, unsigned& err) {
+    using R = float;
+    const R dt = v.dtf;
+    const R invmi = o.vi.w;
+    float4 vl = o.vl, wl = o.wl;
+    float nvx = o.vi.x, nvy = o.vi.y, nvz = o.vi.z;
+    pair_add(nvx, vl.x, (F.fx * invmi + v.gxf) * dt);
+    pair_add(nvy, vl.y, (F.fy * invmi + v.gyf) * dt);
+    pair_add(nvz, vl.z, (F.fz * invmi + v.gzf) * dt);
+    // displacement v*dt as a float pair (the product's rounding error by FMA)
+    const R sx = nvx * dt, sy = nvy * dt, sz = nvz * dt;
+    const R ex_ = fmaf(nvx, dt, -sx) + vl.x * dt;
+    const R ey_ = fmaf(nvy, dt, -sy) + vl.y * dt;
+    const R ez_ = fmaf(nvz, dt, -sz) + vl.z * dt;
+    float4 nh = o.hi, nl = o.li;
+    pair_add(nh.x, nl.x, sx);
+    pair_add(nh.y, nl.y, sy);
+    pair_add(nh.z, nl.z, sz);
+    nl.x += ex_;
+    nl.y += ey_;
+    nl.z += ez_;
+    float nwx = o.wi.x, nwy = o.wi.y, nwz = o.wi.z;
+    pair_add(nwx, wl.x, F.mx * invmoi * dt);
+    pair_add(nwy, wl.y, F.my * invmoi * dt);
+    pair_add(nwz, wl.z, F.mz * invmoi * dt);
+    B.vell[i] = vl;
+    B.rotl[i] = wl;
+    // refresh test against the position of the last rebuild, on the high
+    // parts: it only decides when the lists are rebuilt, and the threshold
+    // leaves a margin of skin/2 to the list cutoff
+    {
+        const R ex = nh.x - o.rh.x, ey = nh.y - o.rh.y, ez = nh.z - o.rh.z;
+        refresh = ex * ex + ey * ey + ez * ez > v.thresh_sqf;
+    }
+    // out of bounds (the box rounded outwards to FP32)
+    R status = 1.f;
+    if (nh.x < v.boxf[0] || nh.x > v.boxf[3] || nh.y < v.boxf[1] || nh.y > v.boxf[4] || nh.z < v.boxf[2] ||
+        nh.z > v.boxf[5])
+        status = 2.f;
+    if (!(nvx == nvx && nvy == nvy && nvz == nvz)) {
+        err |= 0x20u;
+        status = 2.f;
+    }
+    nl.w = status;
+    B.posh[i] = nh;
+    B.posl[i] = nl;
+    B.vel[i] = make_float4(nvx, nvy, nvz, invmi);
+    B.rot[i] = make_float4(nwx, nwy, nwz, status);
+    if (v.store_forces) {
+        v.fx[i] = F.fx; v.fy[i] = F.fy; v.fz[i] = F.fz;
+        v.tx[i] = F.mx; v.ty[i] = F.my; v.tz[i] = F.mz;
+    }
+}
+
+// One particle's step, one thread: particle contacts in row order (the row
+// read four entries at a time so their gathers are in flight together), wall
+// contacts, integration.  Writes bank s^1 and the history.
 template <int MODEL, int WCAP>
 __device__ __forceinline__ void step_one(const View<Mixed>& v, const SBank<Mixed>& A, const SBank<Mixed>& B,
-                                         const PBank<Mixed>& P, int i, Own o, bool& refresh, unsigned& err,
+                                         const PBank<Mixed>& P, int i, const Own& o, bool& refresh, unsigned& err,
                                          const int* nei_s = nullptr, int nei_s_rows = 0) {
     using T = Mixed;
     using R = float;
+    if (o.wi.w != 1.f) {
+        freeze_one(v, B, i, o);
+        return;
+    }
     const int n = v.n;
     const float4* __restrict__ Aposh = A.posh;
     const float4* __restrict__ Aposl = A.posl;
     const float4* __restrict__ Avel = A.vel;
     const float4* __restrict__ Arot = A.rot;
     const int* __restrict__ nei = v.nei;
-    const int* __restrict__ neiw = v.neiw;
-    const int* __restrict__ pid = P.pid;
-    float4 wi = o.wi;
-    const float4 hi = o.hi;
-    float4 li = o.li;
-    const float4 vi = o.vi;
-    float4 vl = o.vl;
-    float4 wl = o.wl;
-    if (wi.w != 1.f) {
-        // inactive, or left the box last step (status 2): frozen from now on
-        B.posh[i] = hi;
-        li.w = 0.f;
-        B.posl[i] = li;
-        B.vel[i] = vi;
-        B.vell[i] = vl;
-        B.rotl[i] = wl;
-        wi.w = 0.f;
-        B.rot[i] = wi;
-        if (v.store_forces) {
-            v.fx[i] = 0.; v.fy[i] = 0.; v.fz[i] = 0.;
-            v.tx[i] = 0.; v.ty[i] = 0.; v.tz[i] = 0.;
+    const float4 hi = o.hi, li = o.li;
+    const R ri = hi.w;
+    const R invmi = o.vi.w;
+    const Mat mt = own_material<MODEL>(P, i, ri, invmi);
+    Force6 F = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    int nc = o.nc;
+    const int nn = o.nn;
+    unsigned long long touched = 0ull;
+    for (int k0 = 0; k0 < nn; k0 += 4) {
+        int jj[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int k = k0 + q;
+            jj[q] = k < nn ? (k < nei_s_rows ? nei_s[k * 32] : __ldg(&nei[(size_t)k * n + i])) : -1;
         }
-    } else {
-        const float4 rh = o.rh;
-        const int nn = o.nn;
-        const int nw = o.nw;
-        int nc = o.nc;
-        int ncw = o.ncw;
-        const R ri = hi.w;
-        const R invmi = vi.w;
-        R ki = 0.f, etai = 0.f, sqrtmi = 0.f, invmoi;
-        if (MODEL == 0) {
-            const float4 mi = __ldg(&P.mat[i]);
-            ki = mi.x; etai = mi.y; sqrtmi = mi.z; invmoi = mi.w;
-        } else {
-            invmoi = 2.5f * invmi / (ri * ri);  // 1 / (2/5 m r^2)
-        }
-        const R dt = v.dtf, mu = v.muf;
-        R fx = 0.f, fy = 0.f, fz = 0.f;
-        R mx = 0.f, my = 0.f, mz = 0.f;
-
-        // ---------------- particle-particle.  The row is read four
-        // entries at a time so their gathers are in flight together; the
-        // contacts among them are then handled one by one in row order.
-        unsigned long long touched = 0ull;
-        for (int k0 = 0; k0 < nn; k0 += 4) {
-            int jj[4];
+        float4 hj[4], lj[4];
 #pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const int k = k0 + q;
-                jj[q] = k < nn ? (k < nei_s_rows ? nei_s[k * 32] : __ldg(&nei[(size_t)k * n + i])) : -1;
-            }
-            float4 hj[4], lj[4];
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-                if (jj[q] >= 0) {
-                    hj[q] = __ldg(&Aposh[jj[q]]);
-                    lj[q] = __ldg(&Aposl[jj[q]]);
-                }
-            }
-            unsigned hit = 0u;
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-                if (jj[q] < 0 || lj[q].w != 1.f) continue;
-                const R dx = (hi.x - hj[q].x) + (li.x - lj[q].x);
-                const R dy = (hi.y - hj[q].y) + (li.y - lj[q].y);
-                const R dz = (hi.z - hj[q].z) + (li.z - lj[q].z);
-                const R Rs = ri + hj[q].w;
-                if (dx * dx + dy * dy + dz * dz < Rs * Rs) hit |= 1u << q;
-            }
-            while (hit) {
-                const int q = __ffs(hit) - 1;
-                hit &= hit - 1u;
-                const int k = k0 + q;
-                const int j = k < nei_s_rows ? nei_s[k * 32] : __ldg(&nei[(size_t)k * n + i]);
-                const float4 hjq = __ldg(&Aposh[j]), ljq = __ldg(&Aposl[j]);
-                const R dx = (hi.x - hjq.x) + (li.x - ljq.x);
-                const R dy = (hi.y - hjq.y) + (li.y - ljq.y);
-                const R dz = (hi.z - hjq.z) + (li.z - ljq.z);
-                const R distsq = dx * dx + dy * dy + dz * dz;
-                const R rj = hjq.w;
-                const R Rs = ri + rj;
-                const float4 vj = __ldg(&Avel[j]);
-                const float4 wj = __ldg(&Arot[j]);
-                const R dist = sqrtf(distsq);
-                const R inv = 1.f / dist;
-                const R delMag = Rs - dist;
-                const R nx = dx * inv, ny = dy * inv, nz = dz * inv;
-                const R vrx = vi.x - vj.x, vry = vi.y - vj.y, vrz = vi.z - vj.z;
-                const R vdn = vrx * nx + vry * ny + vrz * nz;
-                const R vnx = vdn * nx, vny = vdn * ny, vnz = vdn * nz;
-                R fnx, fny, fnz, kt, gt, Rstar = 0.f;
-                if (MODEL == 0) {
-                    const R meff = 1.f / (invmi + vj.w);
-                    const R eta = etai * sqrtf(meff);
-                    const R fel = ki * delMag;
-                    fnx = fel * nx - eta * vnx;
-                    fny = fel * ny - eta * vny;
-                    fnz = fel * nz - eta * vnz;
-                    kt = ki;
-                    gt = eta;
-                } else {
-                    Rstar = ri * rj / Rs;
-                    const R mstar = 1.f / (invmi + vj.w);
-                    const R sqrtRd = sqrtf(Rstar * delMag);
-                    const R fel = v.kn_cf * sqrtRd * delMag;
-                    const R gn = v.damp_cf * sqrtf(v.sn_cf * sqrtRd * mstar);
-                    const R fnm = fel - gn * vdn;
-                    fnx = fnm * nx;
-                    fny = fnm * ny;
-                    fnz = fnm * nz;
-                    kt = v.kt_cf * sqrtRd;
-                    gt = v.damp_cf * sqrtf(kt * mstar);
-                }
-                const R ax_ = ri * wi.x + rj * wj.x;
-                const R ay_ = ri * wi.y + rj * wj.y;
-                const R az_ = ri * wi.z + rj * wj.z;
-                const R vtx = (vrx - vnx) + (ay_ * nz - az_ * ny);
-                const R vty = (vry - vny) + (az_ * nx - ax_ * nz);
-                const R vtz = (vrz - vnz) + (ax_ * ny - ay_ * nx);
-                fx += fnx;
-                fy += fny;
-                fz += fnz;
-                const int pj = __ldg(&pid[j]);
-                bool fresh;
-                const int slot = find_slot<T>(P.hid, n, i, nc, pj, v.hist_cap, fresh);
-                if (slot < 0) {
-                    err |= 0x4u;
-                    continue;
-                }
-                const size_t h = (size_t)slot * n + i;
-                Vec3<R> sp, cp;
-                if (fresh) {
-                    P.hid[h] = pj;
-                    sp.x = sp.y = sp.z = 0.f;
-                    cp.x = cp.y = cp.z = 0.f;
-                } else {
-                    sp.x = P.hx[h]; sp.y = P.hy[h]; sp.z = P.hz[h];
-                    cp.x = P.cx[h]; cp.y = P.cy[h]; cp.z = P.cz[h];
-                }
-                touched |= 1ull << slot;
-                Vec3<R> ft;
-                const R fnsq = fnx * fnx + fny * fny + fnz * fnz;
-                tangential<T>(nx, ny, nz, fnsq, vtx, vty, vtz, gt, kt, mu, dt, sp, cp, ft);
-                fx += ft.x;
-                fy += ft.y;
-                fz += ft.z;
-                mx += ri * (ny * ft.z - nz * ft.y);
-                my += ri * (nz * ft.x - nx * ft.z);
-                mz += ri * (nx * ft.y - ny * ft.x);
-                if (MODEL == 1 && v.mu_rollf > 0.f) {
-                    const R rx = wi.x - wj.x, ry = wi.y - wj.y, rz = wi.z - wj.z;
-                    const R wn2 = rx * rx + ry * ry + rz * rz;
-                    if (wn2 > 0.f) {
-                        const R tr = -v.mu_rollf * Rstar * sqrtf(fnsq) * rsqrtf(wn2);
-                        mx += tr * rx;
-                        my += tr * ry;
-                        mz += tr * rz;
-                    }
-                }
-                P.hx[h] = sp.x; P.hy[h] = sp.y; P.hz[h] = sp.z;
-                P.cx[h] = cp.x; P.cy[h] = cp.y; P.cz[h] = cp.z;
+        for (int q = 0; q < 4; q++) {
+            if (jj[q] >= 0) {
+                hj[q] = __ldg(&Aposh[jj[q]]);
+                lj[q] = __ldg(&Aposl[jj[q]]);
             }
         }
-        P.nc[i] = surviving(touched, nc);
-
-        // ---------------- particle-wall
-        unsigned long long wtouched = 0ull;
-        int vore[WCAP];
-        int nvore = 0;
-        const float3 ph = make_float3(hi.x, hi.y, hi.z), pl = make_float3(li.x, li.y, li.z);
-        const R rsq = ri * ri;
-        for (int kk = 0; kk < nw; kk++) {
-            const int t = __ldg(&neiw[(size_t)kk * n + i]);
-            const FeatureF f = closest_feature_f(ph, pl, rsq, v.trif[t]);
-            if (!(f.dist < ri)) continue;
-            if (f.hit != -1) {
-                bool dup = false;
-                for (int q = 0; q < nvore; q++)
-                    if (vore[q] == f.hit) {
-                        dup = true;
-                        break;
-                    }
-                if (dup) continue;
-                if (nvore < WCAP) vore[nvore++] = f.hit;
-            }
-            const R delmag = ri - f.dist;
-            const R nx = f.nx, ny = f.ny, nz = f.nz;
-            const R vdn = vi.x * nx + vi.y * ny + vi.z * nz;
-            const R vnx = vdn * nx, vny = vdn * ny, vnz = vdn * nz;
-            R fnx, fny, fnz, kt, gt;
-            if (MODEL == 0) {
-                const R eta = etai * sqrtmi;
-                const R fel = ki * delmag;
-                fnx = fel * nx - eta * vnx;
-                fny = fel * ny - eta * vny;
-                fnz = fel * nz - eta * vnz;
-                kt = ki;
-                gt = eta;
-            } else {
-                const R mstar = 1.f / invmi;
-                const R sqrtRd = sqrtf(ri * delmag);
-                const R fel = v.kn_cf * sqrtRd * delmag;
-                const R gn = v.damp_cf * sqrtf(v.sn_cf * sqrtRd * mstar);
-                const R fnm = fel - gn * vdn;
-                fnx = fnm * nx;
-                fny = fnm * ny;
-                fnz = fnm * nz;
-                kt = v.kt_cf * sqrtRd;
-                gt = v.damp_cf * sqrtf(kt * mstar);
-            }
-            const R ax_ = ri * wi.x, ay_ = ri * wi.y, az_ = ri * wi.z;
-            const R vtx = (vi.x - vnx) + (ay_ * nz - az_ * ny);
-            const R vty = (vi.y - vny) + (az_ * nx - ax_ * nz);
-            const R vtz = (vi.z - vnz) + (ax_ * ny - ay_ * nx);
-            fx += fnx;
-            fy += fny;
-            fz += fnz;
+        unsigned hit = 0u;
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            if (jj[q] < 0 || lj[q].w != 1.f) continue;
+            const R dx = (hi.x - hj[q].x) + (li.x - lj[q].x);
+            const R dy = (hi.y - hj[q].y) + (li.y - lj[q].y);
+            const R dz = (hi.z - hj[q].z) + (li.z - lj[q].z);
+            const R Rs = ri + hj[q].w;
+            if (dx * dx + dy * dy + dz * dz < Rs * Rs) hit |= 1u << q;
+        }
+        while (hit) {
+            const int q = __ffs(hit) - 1;
+            hit &= hit - 1u;
+            const int k = k0 + q;
+            const int j = k < nei_s_rows ? nei_s[k * 32] : __ldg(&nei[(size_t)k * n + i]);
+            const float4 hjq = __ldg(&Aposh[j]), ljq = __ldg(&Aposl[j]);
+            const R dx = (hi.x - hjq.x) + (li.x - ljq.x);
+            const R dy = (hi.y - hjq.y) + (li.y - ljq.y);
+            const R dz = (hi.z - hjq.z) + (li.z - ljq.z);
             bool fresh;
-            const int slot = find_slot<T>(P.hwid, n, i, ncw, t, v.histw_cap, fresh);
+            const int slot = find_slot<T>(P.hid, n, i, nc, j, v.hist_cap, fresh);
             if (slot < 0) {
-                err |= 0x8u;
+                err |= 0x4u;
                 continue;
             }
             const size_t h = (size_t)slot * n + i;
             Vec3<R> sp, cp;
             if (fresh) {
-                P.hwid[h] = t;
+                P.hid[h] = j;
                 sp.x = sp.y = sp.z = 0.f;
                 cp.x = cp.y = cp.z = 0.f;
             } else {
-                sp.x = P.hwx[h]; sp.y = P.hwy[h]; sp.z = P.hwz[h];
-                cp.x = P.cwx[h]; cp.y = P.cwy[h]; cp.z = P.cwz[h];
+                sp.x = P.hx[h]; sp.y = P.hy[h]; sp.z = P.hz[h];
+                cp.x = P.cx[h]; cp.y = P.cy[h]; cp.z = P.cz[h];
             }
-            wtouched |= 1ull << slot;
-            Vec3<R> ft;
-            const R fnsq = fnx * fnx + fny * fny + fnz * fnz;
-            tangential<T>(nx, ny, nz, fnsq, vtx, vty, vtz, gt, kt, mu, dt, sp, cp, ft);
-            fx += ft.x;
-            fy += ft.y;
-            fz += ft.z;
-            mx += ri * (ny * ft.z - nz * ft.y);
-            my += ri * (nz * ft.x - nx * ft.z);
-            mz += ri * (nx * ft.y - ny * ft.x);
-            if (MODEL == 1 && v.mu_rollf > 0.f) {
-                const R wn2 = wi.x * wi.x + wi.y * wi.y + wi.z * wi.z;
-                if (wn2 > 0.f) {
-                    const R tr = -v.mu_rollf * ri * sqrtf(fnsq) * rsqrtf(wn2);
-                    mx += tr * wi.x;
-                    my += tr * wi.y;
-                    mz += tr * wi.z;
-                }
-            }
-            P.hwx[h] = sp.x; P.hwy[h] = sp.y; P.hwz[h] = sp.z;
-            P.cwx[h] = cp.x; P.cwy[h] = cp.y; P.cwz[h] = cp.z;
-        }
-        P.ncw[i] = surviving(wtouched, ncw);
-
-        // ---------------- symplectic Euler.  Position, velocity and spin
-        // are float pairs, so their many small increments do not round away.
-        float nvx = vi.x, nvy = vi.y, nvz = vi.z;
-        pair_add(nvx, vl.x, (fx * invmi + v.gxf) * dt);
-        pair_add(nvy, vl.y, (fy * invmi + v.gyf) * dt);
-        pair_add(nvz, vl.z, (fz * invmi + v.gzf) * dt);
-        // displacement v*dt as a float pair (the product's rounding error by FMA)
-        const R sx = nvx * dt, sy = nvy * dt, sz = nvz * dt;
-        const R ex_ = fmaf(nvx, dt, -sx) + vl.x * dt;
-        const R ey_ = fmaf(nvy, dt, -sy) + vl.y * dt;
-        const R ez_ = fmaf(nvz, dt, -sz) + vl.z * dt;
-        float4 nh = hi, nl = li;
-        pair_add(nh.x, nl.x, sx);
-        pair_add(nh.y, nl.y, sy);
-        pair_add(nh.z, nl.z, sz);
-        nl.x += ex_;
-        nl.y += ey_;
-        nl.z += ez_;
-        float nwx = wi.x, nwy = wi.y, nwz = wi.z;
-        pair_add(nwx, wl.x, mx * invmoi * dt);
-        pair_add(nwy, wl.y, my * invmoi * dt);
-        pair_add(nwz, wl.z, mz * invmoi * dt);
-        B.vell[i] = vl;
-        B.rotl[i] = wl;
-        // refresh test against the position of the last rebuild, on the
-        // high parts: it only decides when the lists are rebuilt, and the
-        // threshold leaves a margin of skin/2 to the list cutoff
-        {
-            const R ex = nh.x - rh.x, ey = nh.y - rh.y, ez = nh.z - rh.z;
-            refresh = ex * ex + ey * ey + ez * ez > v.thresh_sqf;
-        }
-        // out of bounds (the box rounded outwards to FP32)
-        R status = 1.f;
-        if (nh.x < v.boxf[0] || nh.x > v.boxf[3] || nh.y < v.boxf[1] || nh.y > v.boxf[4] ||
-            nh.z < v.boxf[2] || nh.z > v.boxf[5])
-            status = 2.f;
-        if (!(nvx == nvx && nvy == nvy && nvz == nvz)) {
-            err |= 0x20u;
-            status = 2.f;
-        }
-        nl.w = status;
-        B.posh[i] = nh;
-        B.posl[i] = nl;
-        B.vel[i] = make_float4(nvx, nvy, nvz, invmi);
-        B.rot[i] = make_float4(nwx, nwy, nwz, status);
-        if (v.store_forces) {
-            v.fx[i] = fx; v.fy[i] = fy; v.fz[i] = fz;
-            v.tx[i] = mx; v.ty[i] = my; v.tz[i] = mz;
+            touched |= 1ull << slot;
+            const Force6 G = pair_force<MODEL>(v, dx, dy, dz, ri, hjq.w, o.vi, o.wi, __ldg(&Avel[j]), __ldg(&Arot[j]),
+                                               invmi, mt, sp, cp);
+            F.fx += G.fx; F.fy += G.fy; F.fz += G.fz;
+            F.mx += G.mx; F.my += G.my; F.mz += G.mz;
+            P.hx[h] = sp.x; P.hy[h] = sp.y; P.hz[h] = sp.z;
+            P.cx[h] = cp.x; P.cy[h] = cp.y; P.cz[h] = cp.z;
         }
     }
+    P.nc[i] = surviving(touched, nc);
+    wall_forces<MODEL, WCAP>(v, P, i, o.nw, o.ncw, hi, li, o.vi, o.wi, invmi, mt, F, err);
+    integrate_one(v, B, i, o, mt.invmoi, F, refresh, err);
 }
 
 // One thread per particle, state loaded straight from HBM.
@@ -491,22 +553,11 @@ __global__ void __launch_bounds__(kBlock, MINB) k_step_mixed(View<Mixed> v, cuda
     step_epilogue(ctl, s, refresh, err, cond, use_cond);
 }
 
-// ---------------------------------------------------------------- TMA-staged
-// Persistent variant: each CTA walks tiles of kBlock consecutive particles.
-// The per-particle arrays of a tile are contiguous, so one thread brings a
-// whole tile in with bulk copies (cp.async.bulk, completion counted on an
-// mbarrier) while the CTA works on the previous tile out of the other buffer.
-// The first Verlet-list rows of the next tile are prefetched into L2 the
-// same way.  Every wait on an mbarrier gives up after kSpinLimit tries and
-// sets GDEM_EW_TIMEOUT.
-constexpr int kNeiPrefetchRows = 8;
+// ---------------------------------------------------------------- bulk copies
+// Bulk copies (cp.async.bulk) into shared memory with completion counted on
+// an mbarrier.  Every wait on an mbarrier gives up after kSpinLimit tries and
+// the kernel then sets GDEM_EW_TIMEOUT.
 constexpr unsigned kSpinLimit = 1u << 22;
-
-struct __align__(16) Stage {
-    float4 posh[kBlock], posl[kBlock], vel[kBlock], rot[kBlock], vell[kBlock], rotl[kBlock], refh[kBlock];
-    int nnei[kBlock], nneiw[kBlock], nc[kBlock], ncw[kBlock];
-};
-constexpr int kStageBytes = (int)sizeof(Stage);
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
     return (unsigned)__cvta_generic_to_shared(p);
@@ -542,114 +593,6 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned by
         "l"(src), "r"(bytes), "r"(smem_u32(bar))
         : "memory");
 }
-__device__ __forceinline__ void bulk_prefetch_l2(const void* src, unsigned bytes) {
-    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
-}
-
-// Issue the bulk copies of tile `t` into `st` (one thread).  The tail tile's
-// int arrays are copied in whole 16-byte units: every array is allocated in
-// 256-byte units, so the rounded copy stays inside its allocation.
-__device__ __forceinline__ void issue_tile(const View<Mixed>& v, const SBank<Mixed>& A, const PBank<Mixed>& P,
-                                           int t, Stage* st, unsigned long long* bar) {
-    const int base = t * kBlock;
-    const int cnt = min(kBlock, v.n - base);
-    const unsigned b16 = 16u * (unsigned)cnt;
-    const unsigned b4 = 4u * (unsigned)((cnt + 3) & ~3);
-    mbar_expect_tx(bar, 7u * b16 + 4u * b4);
-    bulk_g2s(st->posh, A.posh + base, b16, bar);
-    bulk_g2s(st->posl, A.posl + base, b16, bar);
-    bulk_g2s(st->vel, A.vel + base, b16, bar);
-    bulk_g2s(st->rot, A.rot + base, b16, bar);
-    bulk_g2s(st->vell, A.vell + base, b16, bar);
-    bulk_g2s(st->rotl, A.rotl + base, b16, bar);
-    bulk_g2s(st->refh, v.refh + base, b16, bar);
-    bulk_g2s(st->nnei, v.nnei + base, b4, bar);
-    bulk_g2s(st->nneiw, v.nneiw + base, b4, bar);
-    bulk_g2s(st->nc, P.nc + base, b4, bar);
-    bulk_g2s(st->ncw, P.ncw + base, b4, bar);
-    // Verlet rows k*n + [base, base+cnt) of the tile, rounded out to 16 bytes
-    // (inside the list's allocation: row 0 starts 1 KiB-aligned, the last row
-    // ends inside the final 256-byte unit)
-    const int rows = min(kNeiPrefetchRows, v.nei_cap);
-    for (int k = 0; k < rows; k++) {
-        const uintptr_t a = (uintptr_t)(v.nei + (size_t)k * v.n + base);
-        const uintptr_t lo = a & ~(uintptr_t)15, hi = (a + 4u * (unsigned)cnt + 15u) & ~(uintptr_t)15;
-        bulk_prefetch_l2((const void*)lo, (unsigned)(hi - lo));
-    }
-}
-
-template <int MODEL, int WCAP>
-__global__ void __launch_bounds__(kBlock, 2) k_step_mixed_tma(View<Mixed> v, cudaGraphConditionalHandle cond,
-                                                             int use_cond) {
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    Stage* stage = reinterpret_cast<Stage*>(smem_raw);
-    __shared__ __align__(8) unsigned long long full[2];
-    Ctl* ctl = v.ctl;
-    const int s = ctl->s, p = ctl->p;
-    const SBank<Mixed> A = v.S[s];
-    const SBank<Mixed> B = v.S[s ^ 1];
-    const PBank<Mixed> P = v.P[p];
-    const int ntiles = (v.n + kBlock - 1) / kBlock;
-    const int tid = threadIdx.x;
-    bool refresh = false;
-    unsigned err = 0u;
-    if (tid == 0) {
-        mbar_init(&full[0], 1);
-        mbar_init(&full[1], 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    __syncthreads();
-    int t = blockIdx.x;
-    if (tid == 0 && t < ntiles) issue_tile(v, A, P, t, &stage[0], &full[0]);
-    bool timed_out = false;
-    int t_it = 0;
-    for (int it = 0; t < ntiles; it++, t += gridDim.x) {
-        t_it = it;
-        const int b = it & 1;
-        const int tn = t + gridDim.x;
-        if (tid == 0 && tn < ntiles) {
-            // the other buffer was released by the barrier that ended the
-            // previous iteration; order those generic reads before the copy
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            issue_tile(v, A, P, tn, &stage[b ^ 1], &full[b ^ 1]);
-        }
-        const bool ok = mbar_wait_bounded(&full[b], (unsigned)(it >> 1) & 1u);
-        if (__syncthreads_or(!ok)) {
-            timed_out = true;
-            break;
-        }
-        const int i = t * kBlock + tid;
-        if (i < v.n) {
-            const Stage& S = stage[b];
-            Own o;
-            o.wi = S.rot[tid];
-            o.hi = S.posh[tid];
-            o.li = S.posl[tid];
-            o.vi = S.vel[tid];
-            o.vl = S.vell[tid];
-            o.wl = S.rotl[tid];
-            o.rh = S.refh[tid];
-            o.nn = S.nnei[tid];
-            o.nw = S.nneiw[tid];
-            o.nc = S.nc[tid];
-            o.ncw = S.ncw[tid];
-            step_one<MODEL, WCAP>(v, A, B, P, i, o, refresh, err);
-        }
-        __syncthreads();
-    }
-    if (timed_out) {
-        err |= 0x80u;
-        // let the copies still in flight (this iteration's tile and the next
-        // one's) land before the CTA's shared memory goes away
-        if (tid == 0) {
-            mbar_wait_bounded(&full[t_it & 1], (unsigned)(t_it >> 1) & 1u);
-            if (t + (int)gridDim.x < ntiles) mbar_wait_bounded(&full[(t_it + 1) & 1], (unsigned)((t_it + 1) >> 1) & 1u);
-        }
-        __syncthreads();
-    }
-    step_epilogue(ctl, s, refresh, err, cond, use_cond);
-}
-
 // ---------------------------------------------------------------- warp-staged
 // Persistent variant with one pipeline per warp: a warp walks sub-tiles of 32
 // consecutive particles, and its lane 0 brings the next sub-tile's arrays and
@@ -766,12 +709,325 @@ __global__ void __launch_bounds__(kBlock, 2) k_step_mixed_wtma(View<Mixed> v, cu
     step_epilogue(ctl, s, refresh, err, cond, use_cond);
 }
 
+// ---------------------------------------------------------------- warp-cooperative
+// The warp-staged pipeline with the particle contacts computed by the whole
+// warp.  Every lane first tests its whole Verlet row (a bit per entry in
+// contact).  Then, kCoopQ contacts per lane at a time, it finds their history
+// slots in row order (the slot search reads the row's first kHidStageRows
+// history keys from shared memory) and queues them; the warp computes the
+// queued contacts 32 at a time, whoever owns them, and each lane adds its
+// own contacts' results back in row order.  The contact
+// law runs with every lane busy, and its gathers and history loads are in
+// flight together instead of one contact after another.  Shared memory per
+// warp is kept small (two stage buffers and the queue) so that many warps
+// share an SM.
+constexpr int kHidStageRows = 8;
+constexpr int kCoopWarps = 4;
+constexpr int kCoopQ = 4;
+
+struct __align__(16) CStage {
+    float4 posh[32], posl[32], vel[32], rot[32];
+    int nnei[32], nneiw[32], nc[32], ncw[32];
+    int nei[kNeiStageRows][32];
+    int hid[kHidStageRows][32];
+};
+static_assert(sizeof(CStage) % 16 == 0, "stage buffers must keep 16-byte alignment");
+
+struct __align__(16) CQueue {
+    int j[kCoopQ][32];
+    int slot[kCoopQ][32];     // history slot | fresh << 30
+    int who[kCoopQ * 32];     // queue position -> owning lane | its queue row << 8
+    float f[kCoopQ][6][32];   // force and torque of each queued contact
+};
+
+constexpr size_t kCoopSmem = 2 * kCoopWarps * sizeof(CStage) + kCoopWarps * sizeof(CQueue);
+
+__device__ __forceinline__ void bulk_prefetch_l2(const void* src, unsigned bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
+
+// Bulk copies of sub-tile `t` into `st` (lane 0): positions, velocities,
+// spins and counts, plus the first Verlet rows and history-key rows when
+// every row k*n + 32t starts 16-byte aligned (n a multiple of 4).  The
+// arrays read only at the end of the sub-tile (low parts, reference
+// positions) are prefetched into L2.
+__device__ __forceinline__ void issue_csub(const View<Mixed>& v, const SBank<Mixed>& A, const PBank<Mixed>& P,
+                                           int t, CStage* st, unsigned long long* bar, int nei_rows,
+                                           int hid_rows) {
+    const int base = t * 32;
+    const int cnt = min(32, v.n - base);
+    const unsigned b16 = 16u * (unsigned)cnt;
+    const unsigned b4 = 4u * (unsigned)((cnt + 3) & ~3);
+    mbar_expect_tx(bar, 4u * b16 + (4u + (unsigned)nei_rows + (unsigned)hid_rows) * b4);
+    bulk_g2s(st->posh, A.posh + base, b16, bar);
+    bulk_g2s(st->posl, A.posl + base, b16, bar);
+    bulk_g2s(st->vel, A.vel + base, b16, bar);
+    bulk_g2s(st->rot, A.rot + base, b16, bar);
+    bulk_g2s(st->nnei, v.nnei + base, b4, bar);
+    bulk_g2s(st->nneiw, v.nneiw + base, b4, bar);
+    bulk_g2s(st->nc, P.nc + base, b4, bar);
+    bulk_g2s(st->ncw, P.ncw + base, b4, bar);
+    for (int k = 0; k < nei_rows; k++) bulk_g2s(st->nei[k], v.nei + (size_t)k * v.n + base, b4, bar);
+    for (int k = 0; k < hid_rows; k++) bulk_g2s(st->hid[k], P.hid + (size_t)k * v.n + base, b4, bar);
+    bulk_prefetch_l2(A.vell + base, b16);
+    bulk_prefetch_l2(A.rotl + base, b16);
+    bulk_prefetch_l2(v.refh + base, b16);
+}
+
+// History slot of `key` in row i (find_slot) with the first `rows` keys of
+// the row read from shared memory (hid_s, stride 32).  A new key is written
+// to both copies.
+__device__ __forceinline__ int find_slot_staged(int* hid_s, int rows, int* hid, int n, int i, int& nc, int key,
+                                                int cap, bool& fresh) {
+    for (int q = 0; q < nc; q++) {
+        const int h = q < rows ? hid_s[q * 32] : hid[(size_t)q * n + i];
+        if (h == key) {
+            fresh = false;
+            return q;
+        }
+    }
+    fresh = true;
+    if (nc >= cap) return -1;
+    const int q = nc++;
+    hid[(size_t)q * n + i] = key;
+    if (q < rows) hid_s[q * 32] = key;
+    return q;
+}
+
+template <int MODEL, int WCAP, int MINB>
+__global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<Mixed> v, cudaGraphConditionalHandle cond,
+                                                                    int use_cond) {
+    using R = float;
+    constexpr int Q = kCoopQ;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    CStage* stage = reinterpret_cast<CStage*>(smem_raw) + 2 * warp;
+    CQueue* que = reinterpret_cast<CQueue*>(smem_raw + 2 * kCoopWarps * sizeof(CStage)) + warp;
+    __shared__ __align__(8) unsigned long long full[kCoopWarps][2];
+    Ctl* ctl = v.ctl;
+    const int s = ctl->s, p = ctl->p;
+    const SBank<Mixed> A = v.S[s];
+    const SBank<Mixed> B = v.S[s ^ 1];
+    const PBank<Mixed> P = v.P[p];
+    const float4* __restrict__ Aposh = A.posh;
+    const float4* __restrict__ Aposl = A.posl;
+    const float4* __restrict__ Avel = A.vel;
+    const float4* __restrict__ Arot = A.rot;
+    const int* __restrict__ nei = v.nei;
+    const int n = v.n;
+    const int nsub = (n + 31) / 32;
+    const int nei_rows = (n % 4 == 0) ? min(kNeiStageRows, v.nei_cap) : 0;
+    const int hid_rows = (n % 4 == 0) ? min(kHidStageRows, v.hist_cap) : 0;
+    bool refresh = false;
+    unsigned err = 0u;
+    if (lane == 0) {
+        mbar_init(&full[warp][0], 1);
+        mbar_init(&full[warp][1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncwarp();
+    // sub-tiles are handed out one at a time from a counter, so warps that
+    // meet dense sub-tiles (many contacts, many wall candidates) take fewer
+    int t = 0;
+    if (lane == 0) {
+        t = (int)atomicAdd(&ctl->work, 1u);
+        if (t < nsub) issue_csub(v, A, P, t, &stage[0], &full[warp][0], nei_rows, hid_rows);
+    }
+    t = __shfl_sync(0xffffffffu, t, 0);
+    bool timed_out = false;
+    int t_it = 0, t_next = nsub;
+    for (int it = 0; t < nsub; it++, t = t_next) {
+        t_it = it;
+        const int b = it & 1;
+        int tn = 0;
+        if (lane == 0) tn = (int)atomicAdd(&ctl->work, 1u);
+        tn = __shfl_sync(0xffffffffu, tn, 0);
+        t_next = tn;
+        if (lane == 0 && tn < nsub) {
+            // the other buffer was last read before the __syncwarp that ended
+            // the previous iteration; order those reads before the copy
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue_csub(v, A, P, tn, &stage[b ^ 1], &full[warp][b ^ 1], nei_rows, hid_rows);
+        }
+        const bool ok = mbar_wait_bounded(&full[warp][b], (unsigned)(it >> 1) & 1u);
+        if (__any_sync(0xffffffffu, !ok)) {
+            timed_out = true;
+            break;
+        }
+        CStage& S = stage[b];
+        const int i = t * 32 + lane;
+        const bool valid = i < n;
+        const bool active = valid && S.rot[lane].w == 1.f;
+        if (valid && !active) {
+            Own o;
+            o.wi = S.rot[lane];
+            o.hi = S.posh[lane];
+            o.li = S.posl[lane];
+            o.vi = S.vel[lane];
+            o.vl = __ldg(&A.vell[i]);
+            o.wl = __ldg(&A.rotl[i]);
+            freeze_one(v, B, i, o);
+        }
+        Force6 F = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        int nc = S.nc[lane];
+        unsigned long long touched = 0ull;
+        const int nn = active ? S.nnei[lane] : 0;
+        int* hid_s = &S.hid[0][lane];
+        const int* nei_s = &S.nei[0][lane];
+        // ---- this lane's whole row in one pass, four entries at a time with
+        // their gathers in flight together: a bit per row entry in contact
+        unsigned long long hit_lo = 0ull, hit_hi = 0ull;
+        {
+            const float4 hi = S.posh[lane], li = S.posl[lane];
+            for (int k0 = 0; k0 < nn; k0 += 4) {
+                int jj[4];
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const int k = k0 + q;
+                    jj[q] = k < nn ? (k < nei_rows ? nei_s[k * 32] : __ldg(&nei[(size_t)k * n + i])) : -1;
+                }
+                float4 hj[4], lj[4];
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    if (jj[q] >= 0) {
+                        hj[q] = __ldg(&Aposh[jj[q]]);
+                        lj[q] = __ldg(&Aposl[jj[q]]);
+                    }
+                }
+                unsigned hit = 0u;
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    if (jj[q] < 0 || lj[q].w != 1.f) continue;
+                    const R dx = (hi.x - hj[q].x) + (li.x - lj[q].x);
+                    const R dy = (hi.y - hj[q].y) + (li.y - lj[q].y);
+                    const R dz = (hi.z - hj[q].z) + (li.z - lj[q].z);
+                    const R Rs = hi.w + hj[q].w;
+                    if (dx * dx + dy * dy + dz * dz < Rs * Rs) hit |= 1u << q;
+                }
+                if (k0 < 64)
+                    hit_lo |= (unsigned long long)hit << k0;
+                else
+                    hit_hi |= (unsigned long long)hit << (k0 - 64);
+            }
+        }
+        while (true) {
+            // ---- the next (up to) Q contacts of this lane, in row order:
+            // their partners and history slots, queued
+            int cnt = 0;
+#pragma unroll 1
+            for (int q = 0; q < Q && (hit_lo | hit_hi) != 0ull; q++) {
+                int k;
+                if (hit_lo) {
+                    k = __ffsll((long long)hit_lo) - 1;
+                    hit_lo &= hit_lo - 1ull;
+                } else {
+                    k = 64 + __ffsll((long long)hit_hi) - 1;
+                    hit_hi &= hit_hi - 1ull;
+                }
+                const int j = k < nei_rows ? nei_s[k * 32] : __ldg(&nei[(size_t)k * n + i]);
+                bool fresh;
+                const int slot = find_slot_staged(hid_s, hid_rows, P.hid, n, i, nc, j, v.hist_cap, fresh);
+                if (slot < 0) {
+                    err |= 0x4u;
+                    continue;
+                }
+                touched |= 1ull << slot;
+                que->j[cnt][lane] = j;
+                que->slot[cnt][lane] = slot | (fresh ? (1 << 30) : 0);
+                cnt++;
+            }
+            // ---- the warp computes every queued contact
+            int excl = cnt;
+#pragma unroll
+            for (int o2 = 1; o2 < 32; o2 <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, excl, o2);
+                if (lane >= o2) excl += y;
+            }
+            const int total = __shfl_sync(0xffffffffu, excl, 31);
+            excl -= cnt;
+            for (int r = 0; r < cnt; r++) que->who[excl + r] = lane | (r << 8);
+            __syncwarp();
+            for (int w = lane; w < total; w += 32) {
+                const int wh = que->who[w];
+                const int ow = wh & 0xff, r = wh >> 8;
+                const int j = que->j[r][ow];
+                const int sl = que->slot[r][ow];
+                const int slot = sl & 0x3fffffff;
+                const int iow = t * 32 + ow;
+                const float4 hiw = S.posh[ow], liw = S.posl[ow], viw = S.vel[ow], wiw = S.rot[ow];
+                const float4 hjq = __ldg(&Aposh[j]), ljq = __ldg(&Aposl[j]);
+                const float4 vj = __ldg(&Avel[j]), wj = __ldg(&Arot[j]);
+                const size_t h = (size_t)slot * n + iow;
+                Vec3<R> sp, cp;
+                if (sl >> 30) {
+                    sp.x = sp.y = sp.z = 0.f;
+                    cp.x = cp.y = cp.z = 0.f;
+                } else {
+                    sp.x = P.hx[h]; sp.y = P.hy[h]; sp.z = P.hz[h];
+                    cp.x = P.cx[h]; cp.y = P.cy[h]; cp.z = P.cz[h];
+                }
+                const R dx = (hiw.x - hjq.x) + (liw.x - ljq.x);
+                const R dy = (hiw.y - hjq.y) + (liw.y - ljq.y);
+                const R dz = (hiw.z - hjq.z) + (liw.z - ljq.z);
+                const Mat mo = own_material<MODEL>(P, iow, hiw.w, viw.w);
+                const Force6 G = pair_force<MODEL>(v, dx, dy, dz, hiw.w, hjq.w, viw, wiw, vj, wj, viw.w, mo, sp, cp);
+                P.hx[h] = sp.x; P.hy[h] = sp.y; P.hz[h] = sp.z;
+                P.cx[h] = cp.x; P.cy[h] = cp.y; P.cz[h] = cp.z;
+                que->f[r][0][ow] = G.fx;
+                que->f[r][1][ow] = G.fy;
+                que->f[r][2][ow] = G.fz;
+                que->f[r][3][ow] = G.mx;
+                que->f[r][4][ow] = G.my;
+                que->f[r][5][ow] = G.mz;
+            }
+            __syncwarp();
+            // each lane adds its own contacts' results in row order
+            for (int r = 0; r < cnt; r++) {
+                F.fx += que->f[r][0][lane];
+                F.fy += que->f[r][1][lane];
+                F.fz += que->f[r][2][lane];
+                F.mx += que->f[r][3][lane];
+                F.my += que->f[r][4][lane];
+                F.mz += que->f[r][5][lane];
+            }
+            __syncwarp();
+            if (!__any_sync(0xffffffffu, (hit_lo | hit_hi) != 0ull)) break;
+        }
+        if (active) {
+            P.nc[i] = surviving(touched, nc);
+            Own o;
+            o.wi = S.rot[lane];
+            o.hi = S.posh[lane];
+            o.li = S.posl[lane];
+            o.vi = S.vel[lane];
+            const R invmi = o.vi.w;
+            const Mat mt = own_material<MODEL>(P, i, o.hi.w, invmi);
+            wall_forces<MODEL, WCAP>(v, P, i, S.nneiw[lane], S.ncw[lane], o.hi, o.li, o.vi, o.wi, invmi, mt, F, err);
+            o.vl = __ldg(&A.vell[i]);
+            o.wl = __ldg(&A.rotl[i]);
+            o.rh = __ldg(&v.refh[i]);
+            integrate_one(v, B, i, o, mt.invmoi, F, refresh, err);
+        }
+        __syncwarp();
+    }
+    if (timed_out) {
+        err |= 0x80u;
+        // let the copies still in flight land before the shared memory goes away
+        if (lane == 0) {
+            mbar_wait_bounded(&full[warp][t_it & 1], (unsigned)(t_it >> 1) & 1u);
+            if (t_next < nsub) mbar_wait_bounded(&full[warp][(t_it + 1) & 1], (unsigned)((t_it + 1) >> 1) & 1u);
+        }
+        __syncwarp();
+    }
+    step_epilogue(ctl, s, refresh, err, cond, use_cond);
+}
+
 namespace {
 // MINB: resident blocks per SM the register allocation of the one-pass
 // kernel is sized for (2, the default: no spills; 3: more warps in flight,
-// with spills).  GDEM_MIXED_MINB picks one.  GDEM_MIXED_KERNEL=cta picks the
-// CTA-staged persistent kernel, =direct the one-pass kernel, instead of the
-// warp-staged persistent one.
+// with spills).  GDEM_MIXED_MINB picks one.  GDEM_MIXED_KERNEL=staged picks
+// the warp-staged persistent kernel, =direct the one-pass kernel, instead of
+// the warp-cooperative one.
 template <int MODEL, int MINB>
 void* direct_kernel_minb(int wall_cap) {
     if (wall_cap <= 16) return (void*)k_step_mixed<MODEL, 16, MINB>;
@@ -787,19 +1043,6 @@ void* direct_kernel(int wall_cap) {
     return minb == 3 ? direct_kernel_minb<MODEL, 3>(wall_cap) : direct_kernel_minb<MODEL, 2>(wall_cap);
 }
 template <int MODEL>
-void* tma_kernel(int wall_cap) {
-    void* fn = wall_cap <= 16   ? (void*)k_step_mixed_tma<MODEL, 16>
-               : wall_cap <= 32 ? (void*)k_step_mixed_tma<MODEL, 32>
-                                : (void*)k_step_mixed_tma<MODEL, 64>;
-    static bool configured[3] = {false, false, false};
-    const int slot = wall_cap <= 16 ? 0 : (wall_cap <= 32 ? 1 : 2);
-    if (!configured[slot]) {
-        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * kStageBytes);
-        configured[slot] = true;
-    }
-    return fn;
-}
-template <int MODEL>
 void* wtma_kernel(int wall_cap) {
     void* fn = wall_cap <= 16   ? (void*)k_step_mixed_wtma<MODEL, 16>
                : wall_cap <= 32 ? (void*)k_step_mixed_wtma<MODEL, 32>
@@ -812,12 +1055,37 @@ void* wtma_kernel(int wall_cap) {
     }
     return fn;
 }
-// 0: warp-staged (default), 1: CTA-staged, 2: direct
+template <int MODEL, int MINB>
+void* coop_kernel_minb(int wall_cap) {
+    void* fn = wall_cap <= 16   ? (void*)k_step_mixed_coop<MODEL, 16, MINB>
+               : wall_cap <= 32 ? (void*)k_step_mixed_coop<MODEL, 32, MINB>
+                                : (void*)k_step_mixed_coop<MODEL, 64, MINB>;
+    static bool configured[3] = {false, false, false};
+    const int slot = wall_cap <= 16 ? 0 : (wall_cap <= 32 ? 1 : 2);
+    if (!configured[slot]) {
+        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCoopSmem);
+        configured[slot] = true;
+    }
+    return fn;
+}
+// resident CTAs per SM the cooperative kernel's registers are sized for
+// (GDEM_COOP_MINB: 4, 5 or 6; 5 by default)
+template <int MODEL>
+void* coop_kernel(int wall_cap) {
+    static const int minb = [] {
+        const char* e = getenv("GDEM_COOP_MINB");
+        const int m = e ? atoi(e) : 5;
+        return m == 4 || m == 6 ? m : 5;
+    }();
+    return minb == 4 ? coop_kernel_minb<MODEL, 4>(wall_cap)
+                     : (minb == 6 ? coop_kernel_minb<MODEL, 6>(wall_cap) : coop_kernel_minb<MODEL, 5>(wall_cap));
+}
+// 0: warp-cooperative (default), 1: warp-staged, 2: direct
 int kernel_kind() {
     static const int k = [] {
         const char* e = getenv("GDEM_MIXED_KERNEL");
         if (e && strcmp(e, "direct") == 0) return 2;
-        if (e && strcmp(e, "cta") == 0) return 1;
+        if (e && strcmp(e, "staged") == 0) return 1;
         return 0;
     }();
     return k;
@@ -837,17 +1105,22 @@ StepLaunch step_launch(const View<Mixed>& v) {
     const int ntiles = (v.n + kBlock - 1) / kBlock;
     const int kind = kernel_kind();
     if (kind == 0) {
+        void* fn = v.mat.model == 1 ? coop_kernel<1>(v.wall_cap) : coop_kernel<0>(v.wall_cap);
+        const size_t smem = kCoopSmem;
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kCoopWarps * 32, smem);
+        if (per_sm < 1) per_sm = 1;
+        const int nsub = (v.n + 31) / 32;
+        const int need = (nsub + kCoopWarps - 1) / kCoopWarps;
+        const int grid = need < per_sm * sm_count() ? need : per_sm * sm_count();
+        return StepLaunch{fn, dim3(grid), dim3(kCoopWarps * 32), smem};
+    }
+    if (kind == 1) {
         void* fn = v.mat.model == 1 ? wtma_kernel<1>(v.wall_cap) : wtma_kernel<0>(v.wall_cap);
         const int nsub = (v.n + 31) / 32;
         const int need = (nsub + kWarps - 1) / kWarps;
         const int grid = need < 2 * sm_count() ? need : 2 * sm_count();
         return StepLaunch{fn, dim3(grid), dim3(kBlock), (size_t)2 * kWarps * kWStageBytes};
-    }
-    if (kind == 1) {
-        void* fn = v.mat.model == 1 ? tma_kernel<1>(v.wall_cap) : tma_kernel<0>(v.wall_cap);
-        // two resident CTAs per SM (registers), each walking its share of tiles
-        const int grid = ntiles < 2 * sm_count() ? ntiles : 2 * sm_count();
-        return StepLaunch{fn, dim3(grid), dim3(kBlock), (size_t)2 * kStageBytes};
     }
     void* fn = v.mat.model == 1 ? direct_kernel<1>(v.wall_cap) : direct_kernel<0>(v.wall_cap);
     return StepLaunch{fn, dim3(ntiles), dim3(kBlock), 0};

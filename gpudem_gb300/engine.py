@@ -48,7 +48,7 @@ class Engine:
     def __init__(self, scene: Scene, precision="fp64", model="linear", reorder=True,
                  store_forces=False, nei_capacity=64, wall_capacity=32, hist_capacity=32,
                  hist_wall_capacity=16, steps_per_graph=8, cell_size=-1.0, skin=None,
-                 refresh=None, box=None):
+                 refresh=None, box=None, bvh_every_step=False):
         self.L = _lib.load()
         self.scene = scene
         self.n = scene.n
@@ -79,6 +79,7 @@ class Engine:
         d.poisson_ratio = scene.nu
         d.restitution = scene.e
         d.rolling_friction = scene.mu_roll
+        d.bvh_every_step = 1 if bvh_every_step else 0
         self.desc = d
         h = C.c_void_p()
         _lib.check(self.L.gdem_create(C.byref(d), C.byref(h)), None, "gdem_create")
@@ -87,7 +88,7 @@ class Engine:
         self.ntri = 0
         if scene.tris is not None and len(scene.tris):
             self.set_mesh(scene.tris)
-        self.import_particles(scene)
+        self.import_particles(scene, history=scene.history, hist_stride=scene.hist_stride)
 
     # ------------------------------------------------------------------ setup
     def _check(self, rc, what):
@@ -115,7 +116,7 @@ class Engine:
         self.ntri = m.nTri
         self._check(self.L.gdem_set_mesh_indexed(self.h, C.byref(m)), "gdem_set_mesh_indexed")
 
-    def import_particles(self, sc: Scene, history=None):
+    def import_particles(self, sc: Scene, history=None, hist_stride=MAX_NEI):
         n = sc.n
         self._keep = []
         arr = lambda a: self._keep.append(np.ascontiguousarray(a, np.float64)) or self._keep[-1]
@@ -128,9 +129,13 @@ class Engine:
         p.m = _ptr(arr(sc.m))
         p.k = _ptr(arr(sc.k))
         p.etaconst = _ptr(arr(sc.eta))
+        if sc.active is not None:
+            act = np.ascontiguousarray(sc.active, np.int32)
+            self._keep.append(act)
+            p.isActive = _ptr(act, C.c_int)
         p.hist_stride = 0
         if history is not None:
-            p.hist_stride = MAX_NEI
+            p.hist_stride = hist_stride
             for nm, v in history.items():
                 a = np.ascontiguousarray(v, np.int32 if nm.startswith(("num", "ind")) else np.float64)
                 self._keep.append(a)
@@ -149,8 +154,9 @@ class Engine:
         self._check(self.L.gdem_rebuild(self.h), "gdem_rebuild")
 
     # ------------------------------------------------------------------ export
-    def export(self, history=True, forces=None):
-        """copyFromDevice (ParticleSystem.cu:97): state in pId order, reference layout."""
+    def export(self, history=True, forces=None, hist_stride=MAX_NEI):
+        """copyFromDevice (ParticleSystem.cu:97): state in pId order, reference
+        layout (history rows of `hist_stride` slots, MAX_NEI by default)."""
         n = self.n
         out = {k: np.zeros(3 * n) for k in ("x", "v", "angv")}
         out["isActive"] = np.zeros(n, np.int32)
@@ -164,15 +170,15 @@ class Engine:
             out["mom"] = np.zeros(3 * n)
             p.f, p.mom = _ptr(out["f"]), _ptr(out["mom"])
         if history:
-            p.hist_stride = MAX_NEI
+            p.hist_stride = hist_stride
             for nm in ("numCont", "numContWall"):
                 out[nm] = np.zeros(n, np.int32)
                 setattr(p, nm, _ptr(out[nm], C.c_int))
             for nm in ("indHis", "indHisWall"):
-                out[nm] = np.full(n * MAX_NEI, -1, np.int32)
+                out[nm] = np.full(n * hist_stride, -1, np.int32)
                 setattr(p, nm, _ptr(out[nm], C.c_int))
             for nm in ("deltHisx", "deltHisy", "deltHisz", "deltHisxWall", "deltHisyWall", "deltHiszWall"):
-                out[nm] = np.zeros(n * MAX_NEI)
+                out[nm] = np.zeros(n * hist_stride)
                 setattr(p, nm, _ptr(out[nm]))
         self._check(self.L.gdem_export_particles(self.h, C.byref(p)), "gdem_export_particles")
         return out

@@ -93,16 +93,27 @@ def tilted_box_mesh(half=0.1, deg=30.0, levels=0) -> np.ndarray:
 
 
 def helical_chute_mesh(radius=0.3, pitch=0.1, turns=2.0, width=0.12, wall=0.05,
-                       n_target=50_000, seed=3) -> np.ndarray:
+                       n_target=50_000, seed=3, inner_wall=False, end_caps=False,
+                       isotropic=False) -> np.ndarray:
     """Parametric helical chute: a ramp winding around the y axis plus an outer
-    side wall, tessellated to about `n_target` triangles.  The ramp surface
-    spans radii [radius-width, radius]; the wall stands `wall` high at the
-    outer radius.  A seeded +-2 % jitter of the ramp's radial samples keeps the
+    side wall (and, with `inner_wall`, an inner one; with `end_caps`, walls
+    closing both ends), tessellated to about `n_target` triangles.  The ramp
+    surface spans radii [radius-width, radius]; the walls stand `wall` high.
+    A seeded +-2 % jitter of the ramp's interior radial samples keeps the
     triangles from being perfectly regular."""
     rng = np.random.default_rng(seed)
     n_r = 6                                   # radial quads on the ramp
-    n_h = 3                                   # vertical quads on the outer wall
-    per_step = 2 * (n_r + n_h)
+    n_h = 3                                   # vertical quads on a side wall
+    if isotropic:
+        # quads about as long as they are wide: side s with
+        # (length along the helix) x (ramp width + walls) = (n_target / 2) s^2
+        r_mid = radius - 0.5 * width
+        length = 2 * math.pi * turns * math.hypot(r_mid, pitch / (2 * math.pi))
+        span = width + wall * (2 if inner_wall else 1)
+        side = math.sqrt(length * span / (0.5 * n_target))
+        n_r = max(1, int(round(width / side)))
+        n_h = max(1, int(round(wall / side)))
+    per_step = 2 * (n_r + n_h * (2 if inner_wall else 1))
     n_t = max(4, int(round(n_target / per_step)))
     th = np.linspace(0.0, 2 * math.pi * turns, n_t + 1)
     y0 = pitch * th / (2 * math.pi)
@@ -125,6 +136,22 @@ def helical_chute_mesh(radius=0.3, pitch=0.1, turns=2.0, width=0.12, wall=0.05,
     for a in range(n_t):
         for b in range(n_h):
             tris += _quad(wallp[a, b], wallp[a + 1, b], wallp[a + 1, b + 1], wallp[a, b + 1])
+    if inner_wall:
+        innp = np.stack([r_in * np.repeat(np.cos(th)[:, None], n_h + 1, 1),
+                         -y0[:, None] + hh[None, :],
+                         r_in * np.repeat(np.sin(th)[:, None], n_h + 1, 1)], -1)
+        for a in range(n_t):
+            for b in range(n_h):
+                tris += _quad(innp[a, b], innp[a + 1, b], innp[a + 1, b + 1], innp[a, b + 1])
+    if end_caps:
+        for a in (0, n_t):
+            c, sn = math.cos(th[a]), math.sin(th[a])
+            for b in range(n_r):
+                for e in range(n_h):
+                    r0, r1 = rr[b], rr[b + 1]
+                    h0, h1 = -y0[a] + hh[e], -y0[a] + hh[e + 1]
+                    tris += _quad(np.array([r0 * c, h0, r0 * sn]), np.array([r1 * c, h0, r1 * sn]),
+                                  np.array([r1 * c, h1, r1 * sn]), np.array([r0 * c, h1, r0 * sn]))
     return np.asarray(tris, dtype=np.float64)
 
 
@@ -242,6 +269,11 @@ class Scene:
     e: float = 0.5
     mu_roll: float = 0.0
     name: str = ""
+    # contact history in the reference layout (numCont, indHis, deltHis*, and
+    # the wall arrays), rows of `hist_stride` slots; None: no contacts yet
+    history: dict | None = None
+    hist_stride: int = 0
+    active: np.ndarray | None = None   # (N,) isActive; None: all active
 
     @property
     def n(self) -> int:
@@ -328,3 +360,82 @@ def config3_helical_chute(n=1_000_000, seed=3, n_tri=50_000, radius=0.3, pitch=0
     return Scene(x=x, r=radii, m=m, k=k, eta=eta_const(k, 0.5), mu=0.5, dt=1e-6,
                  tris=tris, inlet_lo=lo, inlet_hi=hi, v=v, E=5e6, nu=0.3, e=0.5,
                  name=f"helical-chute-{n}")
+
+
+def config3_chute_pour(n=1_000_000, seed=3, n_tri=50_000, radius=0.3, pitch=0.1, width=0.12, turns=3.0,
+                       wall=0.09) -> Scene:
+    """The poured-chute inlet state: 1e6 lognormal spheres (median 1 mm,
+    sigma_log 0.15, clipped [0.6,1.6] mm) on a jittered loose lattice resting
+    just above every turn of a closed helical chute (radius 0.3 m, pitch
+    0.1 m, 3 turns, inner and outer walls 9 cm high, end walls, ~5e4
+    triangles of about 7 mm), filled from the ramp upwards, at rest.  HM material E=5e6 Pa,
+    nu=0.3, e=0.5, mu=0.5; dt=1e-6 s.  `settle_scene` pours it into a bed."""
+    rng = np.random.default_rng(seed)
+    radii = lognormal_radii(n, rng)
+    tris = helical_chute_mesh(radius=radius, pitch=pitch, turns=turns, width=width, wall=wall,
+                              n_target=n_tri, seed=seed, inner_wall=True, end_caps=True, isotropic=True)
+    rmax = float(radii.max())
+    a = 2.0 * rmax * 1.02
+    r_in, r_out = radius - width + rmax + 2e-3, radius - rmax - 2e-3
+    xs = np.arange(-r_out, r_out + 1e-12, a)
+    X, Z = np.meshgrid(xs, xs, indexing="ij")
+    rr = np.hypot(X, Z)
+    keep = (rr >= r_in) & (rr <= r_out)
+    cols = np.stack([X[keep], Z[keep]], 1)
+    th = np.mod(np.arctan2(cols[:, 1], cols[:, 0]), 2 * math.pi)
+    n_turns = int(turns)
+    per_layer = cols.shape[0] * n_turns
+    layers = int(math.ceil(n / per_layer))
+    if (layers - 1) * a + 2 * rmax + 2e-3 > pitch - 2 * rmax:
+        raise ValueError("the lattice does not fit between the chute's turns")
+    site = np.arange(per_layer * layers)
+    lay = site // per_layer
+    rest = site % per_layer
+    turn = rest // cols.shape[0]
+    col = rest % cols.shape[0]
+    # fill the lowest layers first, in a seeded order within the top layer
+    order = np.lexsort((rng.random(site.size), lay))[:n]
+    lay, turn, col = lay[order], turn[order], col[order]
+    ramp_y = -pitch * (th[col] + 2 * math.pi * turn) / (2 * math.pi)
+    x = np.stack([cols[col, 0], ramp_y + rmax + 1e-3 + lay * a, cols[col, 1]], 1)
+    x += (rng.random((n, 3)) - 0.5) * (0.05 * rmax)
+    perm = rng.permutation(n)              # pId order unrelated to position
+    x = x[perm]
+    lo = x.min(0) - rmax
+    hi = x.max(0) + rmax
+    m = sphere_mass(2500.0, radii)
+    k = np.full(n, stiffness_from_E(5e6, 1e-3))
+    return Scene(x=x, r=radii, m=m, k=k, eta=eta_const(k, 0.5), mu=0.5, dt=1e-6,
+                 tris=tris, inlet_lo=lo, inlet_hi=hi, E=5e6, nu=0.3, e=0.5,
+                 name=f"helical-chute-pour-{n}")
+
+
+def settle_scene(sc: Scene, steps=10_000, dt=2e-5, e=0.1, precision="mixed", hist_stride=32,
+                 chunk=1000, log=None) -> Scene:
+    """Pour `sc` into a bed on the GPU: run the engine (Hertz-Mindlin) with a
+    larger time step `dt` and restitution `e` for `steps` steps, then return
+    the scene at that state (positions, velocities, spins, tangential
+    history) with the original time step and material.  Deterministic for a
+    given scene and GPU."""
+    from dataclasses import replace
+    from .engine import Engine
+    pour = replace(sc, dt=dt, e=e, history=None, hist_stride=0)
+    E = Engine(pour, precision=precision, model="hertz_mindlin", hist_capacity=hist_stride,
+               hist_wall_capacity=min(hist_stride, 16))
+    done = 0
+    while done < steps:
+        c = min(chunk, steps - done)
+        E.step(c)
+        done += c
+        if log is not None:
+            st = E.stats()
+            log(f"settle step {done}: active {st['n_active']} KE {st['kinetic_energy']:.3e} "
+                f"contacts/particle {st['coordination']:.2f} rebuilds {st['rebuilds']} error {st['error_word']}")
+    st = E.export(history=True, hist_stride=hist_stride)
+    E.close()
+    hist = {k: st[k] for k in ("numCont", "indHis", "deltHisx", "deltHisy", "deltHisz", "numContWall",
+                               "indHisWall", "deltHisxWall", "deltHisyWall", "deltHiszWall")}
+    act = st["isActive"] == 1
+    return replace(sc, x=st["x"].reshape(-1, 3), v=st["v"].reshape(-1, 3), w=st["angv"].reshape(-1, 3),
+                   history=hist, hist_stride=hist_stride, active=act,
+                   name=sc.name + f"-settled{steps}")

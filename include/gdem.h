@@ -78,6 +78,8 @@ typedef struct gdem_desc {
     double poisson_ratio;
     double restitution;
     double rolling_friction;
+    int bvh_every_step;     /* 1: rebuild the mesh LBVH (keys, sort, nodes, boxes) in every step, as a
+                               moving mesh needs; 0 (default): build it once when the mesh is set */
 } gdem_desc;
 
 /* Particle arrays in the reference layout (memberList/ParticleSystemMember_common.def).

@@ -82,6 +82,27 @@ def test_mixed_close_to_fp64_small(model):
     assert abs(sb["kinetic_energy"] - sa["kinetic_energy"]) <= OBS_RTOL * sa["kinetic_energy"]
 
 
+def test_mixed_history_keys_follow_reorders():
+    """Mixed mode keys its contact history by storage index and remaps the
+    keys when a rebuild reorders the particles; exported, the keys are pIds
+    and the rows match the FP64 engine's (same contacts, encounter order)."""
+    from gpudem_gb300 import engine
+    sc = _hm_scene(20_000, seed=43)
+    A = engine.Engine(sc, precision="fp64", model="hertz_mindlin")
+    B = engine.Engine(sc, precision="mixed", model="hertz_mindlin")
+    for E in (A, B):
+        E.step(60)
+        E.rebuild()          # reorder with live histories
+        E.step(60)
+        E.rebuild()
+        E.step(30)
+    ha, hb = A.export(history=True), B.export(history=True)
+    assert B.stats()["error_word"] == 0
+    assert np.array_equal(ha["numCont"], hb["numCont"])
+    assert np.array_equal(compact_rows(ha["indHis"], ha["numCont"]), compact_rows(hb["indHis"], hb["numCont"]))
+    assert int(ha["numCont"].sum()) > 300
+
+
 # At the benchmark size the largest deviations come from a handful of
 # contacts whose stick/slip decision (|ft| > mu |fn|, a discontinuity of the
 # contact law) falls the other way under FP32 rounding; the bound on the
