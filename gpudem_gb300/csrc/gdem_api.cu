@@ -55,7 +55,8 @@ struct MeshData {
     uint32_t* morton[2] = {nullptr, nullptr};
     int* idx[2] = {nullptr, nullptr};
     uint32_t *hist = nullptr, *tot = nullptr;  // key-sort scratch
-    int* flags = nullptr;                      // refit flags
+    char* seg = nullptr;                       // segment tree of leaf boxes
+    unsigned* done = nullptr;                  // last-CTA counter of the tree build
     double gmin[3] = {0., 0., 0.}, ginv[3] = {0., 0., 0.};
     std::vector<double> aabb_h;
 };
@@ -67,7 +68,7 @@ static void launch_bvh_rebuild(const MeshData& M, cudaStream_t st) {
     launch_tri_keys(M.rec, M.morton[0], M.idx[0], M.ntri, M.gmin, M.ginv, st);
     radix_sort_pairs(M.morton[0], M.idx[0], M.morton[1], M.idx[1], M.hist, M.tot, M.ntri, rs_blocks_for(M.ntri), 0,
                      4, st);
-    launch_bvh_build(M.aabb_d, M.nodes, M.morton[0], M.idx[0], M.flags, M.ntri, st);
+    launch_bvh_build(M.aabb_d, M.nodes, M.morton[0], M.idx[0], M.seg, M.done, M.ntri, st);
 }
 
 // Everything that depends on the precision mode.
@@ -408,8 +409,9 @@ struct Impl : EngineBase {
                     hh[k] = (float)xs[k];
                     ll[k] = (float)(xs[k] - (double)hh[k]);
                 }
-                posh[i] = make_float4(hh[0], hh[1], hh[2], (float)pos[i].w);
-                posl[i] = make_float4(ll[0], ll[1], ll[2], (float)rot[i].w);
+                const float rh = (float)pos[i].w, rl = (float)(pos[i].w - (double)rh);
+                posh[i] = make_float4(hh[0], hh[1], hh[2], rot[i].w == R(1) ? rh : -rh);
+                posl[i] = make_float4(ll[0], ll[1], ll[2], rl);
             }
         }
         const SBank<T>& S = v.S[0];
@@ -533,7 +535,8 @@ struct Impl : EngineBase {
             pos.resize(n);
             for (int i = 0; i < n; i++)
                 pos[i] = make_double4_32a((double)ph[i].x + (double)pl[i].x, (double)ph[i].y + (double)pl[i].y,
-                                          (double)ph[i].z + (double)pl[i].z, (double)ph[i].w);
+                                          (double)ph[i].z + (double)pl[i].z,
+                                          (double)fabsf(ph[i].w) + (double)pl[i].w);
         } else if ((rc = dl(pos, S.pos, n))) {
             return rc;
         }
@@ -982,13 +985,15 @@ static int upload_mesh(gdem_handle* h, const std::vector<double>& vx, const std:
     A.add(&dvx, NV); A.add(&dvy, NV); A.add(&dvz, NV);
     A.add(&draw3, raw3_h ? 3 * (size_t)T : (size_t)T);
     A.add(&dtv, 3 * (size_t)T); A.add(&dte, 3 * (size_t)T);
-    A.add(&M.flags, T);
+    A.add(&M.seg, bvh_scratch_bytes(T));
+    A.add(&M.done, 1);
     A.add(&M.morton[0], T); A.add(&M.morton[1], T);
     A.add(&M.idx[0], T); A.add(&M.idx[1], T);
     A.add(&M.hist, (size_t)256 * nb);
     A.add(&M.tot, 256);
     CK(cudaMalloc((void**)&M.arena, A.total()));
     A.bind(M.arena);
+    CK(cudaMemsetAsync(M.done, 0, sizeof(unsigned), st));
     M.ntri = T;
     CK(cudaMemcpyAsync(dvx, vx.data(), sizeof(double) * NV, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(dvy, vy.data(), sizeof(double) * NV, cudaMemcpyHostToDevice, st));
@@ -1008,7 +1013,7 @@ static int upload_mesh(gdem_handle* h, const std::vector<double>& vx, const std:
         M.ginv[k] = inv[k];
     }
     radix_sort_pairs(M.morton[0], M.idx[0], M.morton[1], M.idx[1], M.hist, M.tot, T, nb, 0, 4, st);
-    launch_bvh_build(M.aabb_d, M.nodes, M.morton[0], M.idx[0], M.flags, T, st);
+    launch_bvh_build(M.aabb_d, M.nodes, M.morton[0], M.idx[0], M.seg, M.done, T, st);
     CK(cudaStreamSynchronize(st));
     CK(cudaGetLastError());
     h->eng->set_mesh(M);

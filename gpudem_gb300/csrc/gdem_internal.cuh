@@ -88,11 +88,12 @@ struct SBank {
     double4_32a* pos;        // FP64 mode: {x, y, z, r}
     typename T::v4* vel;
     typename T::v4* rot;
-    // mixed mode: the positions as unevaluated float pairs x = hi + lo
-    // (|lo| <= ulp(hi)/2, about 48 significant bits), the only copy of the
-    // positions: posh = {hi.xyz, r}, posl = {lo.xyz, status}.  A pair's
-    // relative vector (hi_i - hi_j) + (lo_i - lo_j) is formed at FP64
-    // accuracy with FP32 adds, and hi + lo is exact in FP64.
+    // mixed mode: the positions and radii as unevaluated float pairs
+    // x = hi + lo (|lo| <= ulp(hi)/2, about 48 significant bits), the only
+    // copy of the positions: posh = {hi.xyz, r_hi}, with r_hi negated when
+    // the particle is not active (status != 1), and posl = {lo.xyz, r_lo}.
+    // hi + lo is exact in FP64; a pair's geometry is formed from the pairs
+    // without cancellation error (pair_geometry in the mixed step).
     float4* posh;
     float4* posl;
     // mixed mode: low parts of the velocity and spin float pairs {lo.xyz, 0}
@@ -185,7 +186,7 @@ __device__ __forceinline__ double4_32a load_pos(const SBank<T>& S, int i) {
     if constexpr (T::mixed) {
         const float4 h = S.posh[i], l = S.posl[i];
         return make_double4_32a((double)h.x + (double)l.x, (double)h.y + (double)l.y,
-                                (double)h.z + (double)l.z, (double)h.w);
+                                (double)h.z + (double)l.z, (double)fabsf(h.w) + (double)l.w);
     } else {
         return S.pos[i];
     }
@@ -359,8 +360,12 @@ void launch_finalize_oob(const View<T>& v, cudaStream_t st);
 // k_tri_precompute computes them.
 void launch_tri_keys(const TriRec* rec, uint32_t* morton, int* idx, int ntri, const double* gmin,
                      const double* invrange, cudaStream_t st);
-void launch_bvh_build(const double* aabb, BNode* nodes, const uint32_t* morton_sorted,
-                      const int* sorted_idx, int* flags, int ntri, cudaStream_t st);
+// LBVH of the Morton-sorted triangles: leaves, a segment tree of their boxes
+// in `seg` (bvh_scratch_bytes), internal nodes with their boxes.  `done` is a
+// counter that must start at 0 (it is left at 0).
+void launch_bvh_build(const double* aabb, BNode* nodes, const uint32_t* morton_sorted, const int* sorted_idx,
+                      void* seg, unsigned* done, int ntri, cudaStream_t st);
+size_t bvh_scratch_bytes(int ntri);
 void launch_tri_precompute(TriRec* rec, uint32_t* morton, int* idx, const double* vx,
                            const double* vy, const double* vz, const int* tv, const int* te,
                            const double* raw3, const double* dplane, int ntri, const double* gmin,

@@ -90,6 +90,12 @@ __global__ void __launch_bounds__(1024) k_rs_scan(uint32_t* __restrict__ hist, i
     if (threadIdx.x == 0) tot[blockIdx.x] = carry;
 }
 
+// SMALL: few tiles (nblocks <= RS_SMALL_TILES); the tile counts are then
+// read unscanned and each block sums what it needs itself, with no scan
+// kernel in between.
+constexpr int RS_SMALL_TILES = 32;
+
+template <bool SMALL>
 __global__ void __launch_bounds__(RS_THREADS) k_rs_downsweep(
     const uint32_t* __restrict__ kin, const int* __restrict__ vin, uint32_t* __restrict__ kout,
     int* __restrict__ vout, int n, int shift, const uint32_t* __restrict__ hist,
@@ -101,7 +107,20 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_downsweep(
     __shared__ uint32_t scan_tmp[256];
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     // digit base = exclusive prefix of the digit totals + this tile's offset
-    scan_tmp[t] = tot[t];
+    uint32_t total, mine;
+    if (SMALL) {
+        total = 0u;
+        mine = 0u;
+        for (int b = 0; b < nblocks; b++) {
+            const uint32_t c = hist[t * nblocks + b];
+            if (b < (int)blockIdx.x) mine += c;
+            total += c;
+        }
+    } else {
+        total = tot[t];
+        mine = hist[t * nblocks + blockIdx.x];
+    }
+    scan_tmp[t] = total;
     __syncthreads();
     for (int o = 1; o < 256; o <<= 1) {
         const uint32_t y = t >= o ? scan_tmp[t - o] : 0u;
@@ -109,7 +128,7 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_downsweep(
         scan_tmp[t] += y;
         __syncthreads();
     }
-    base[t] = scan_tmp[t] - tot[t] + hist[t * nblocks + blockIdx.x];
+    base[t] = scan_tmp[t] - total + mine;
 #pragma unroll
     for (int w = 0; w < NW; w++) wcnt[w][t] = 0;
     __syncthreads();
@@ -161,9 +180,14 @@ static void rs_passes(uint32_t* k0, int* v0, uint32_t* k1, int* v1, uint32_t* hi
         const int shift = 8 * (first_pass + p);
         const int a = p & 1;
         k_rs_upsweep<<<nblocks, RS_THREADS, 0, st>>>(ks[a], n, shift, hist, nblocks, ctl, gated);
-        k_rs_scan<<<256, 1024, 0, st>>>(hist, nblocks, tot, ctl, gated);
-        k_rs_downsweep<<<nblocks, RS_THREADS, 0, st>>>(ks[a], vs[a], ks[a ^ 1], vs[a ^ 1], n, shift,
-                                                       hist, tot, nblocks, ctl, gated);
+        if (nblocks <= RS_SMALL_TILES) {
+            k_rs_downsweep<true><<<nblocks, RS_THREADS, 0, st>>>(ks[a], vs[a], ks[a ^ 1], vs[a ^ 1], n, shift,
+                                                                 hist, tot, nblocks, ctl, gated);
+        } else {
+            k_rs_scan<<<256, 1024, 0, st>>>(hist, nblocks, tot, ctl, gated);
+            k_rs_downsweep<false><<<nblocks, RS_THREADS, 0, st>>>(ks[a], vs[a], ks[a ^ 1], vs[a ^ 1], n, shift,
+                                                                  hist, tot, nblocks, ctl, gated);
+        }
     }
 }
 
@@ -204,10 +228,7 @@ __global__ void k_finalize_oob(View<T> v) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.n) return;
     const SBank<T> S = v.S[v.ctl->s];
-    if (S.rot[i].w == 2) {
-        S.rot[i].w = 0;
-        if (T::mixed) S.posl[i].w = 0.f;
-    }
+    if (S.rot[i].w == 2) S.rot[i].w = 0;  // (mixed: posh.w is already negative)
 }
 
 template <class T>
@@ -400,7 +421,7 @@ __global__ void __launch_bounds__(kBlock) k_neighbors(View<T> v, int gated) {
                             const float4 fj = PF[j];
                             const float ex = fi.x - fj.x, ey = fi.y - fj.y, ez = fi.z - fj.z;
                             const float dsqf = ex * ex + ey * ey + ez * ez;
-                            const float Rf = fi.w + fj.w + skinf;
+                            const float Rf = fabsf(fi.w) + fabsf(fj.w) + skinf;
                             const float Rhi = Rf + delta, Rlo = Rf - delta;
                             if (dsqf > Rhi * Rhi * 1.0000039f) continue;  // (1 + 2^-18): surely outside
                             bool inside = Rlo > 0.f && dsqf < Rlo * Rlo * 0.9999962f;  // surely inside
@@ -680,7 +701,118 @@ __device__ __forceinline__ int lbvh_delta(const uint32_t* key, int n, int i, int
     return __clz(a ^ b);
 }
 
-__global__ void k_lbvh_internal(BNode* nodes, const uint32_t* key, int n) {
+// Node boxes without a bottom-up climb: a segment tree over the sorted leaf
+// boxes (level L, node k covers sorted leaves [k 2^L, (k+1) 2^L) ∩ [0, n)),
+// built per 512 leaves in shared memory by one CTA each, the levels above by
+// the last CTA to finish (atomic counter, no waiting).  An internal node's box
+// is then the union over the O(log n) tree nodes covering its leaf range: the
+// same minima and maxima a recursive refit takes, in any order.
+struct __align__(16) SegBox {
+    double lo[3], hi[3];
+};
+
+__host__ __device__ __forceinline__ int seg_count(int n, int level) {
+    return (int)(((long long)n + (1ll << level) - 1) >> level);
+}
+__host__ __device__ __forceinline__ int seg_offset(int n, int level) {
+    int off = 0;
+    for (int L = 0; L < level; L++) off += seg_count(n, L);
+    return off;
+}
+int seg_levels(int n) {
+    int L = 0;
+    while (seg_count(n, L) > 1) L++;
+    return L + 1;
+}
+
+__device__ __forceinline__ SegBox seg_union(const SegBox& a, const SegBox& b) {
+    SegBox c;
+    for (int k = 0; k < 3; k++) {
+        c.lo[k] = a.lo[k] < b.lo[k] ? a.lo[k] : b.lo[k];
+        c.hi[k] = a.hi[k] > b.hi[k] ? a.hi[k] : b.hi[k];
+    }
+    return c;
+}
+
+// boxes written by other CTAs: read through L2
+__device__ __forceinline__ SegBox seg_load_cg(const SegBox* p) {
+    SegBox b;
+    for (int k = 0; k < 3; k++) {
+        b.lo[k] = __ldcg(&p->lo[k]);
+        b.hi[k] = __ldcg(&p->hi[k]);
+    }
+    return b;
+}
+
+constexpr int kSegTile = 512;
+constexpr int kSegTileLevels = 10;  // levels 0..9 inside one CTA's 512 leaves
+
+__global__ void __launch_bounds__(kSegTile) k_lbvh_leaves(BNode* nodes, const double* aabb, const int* sorted_idx,
+                                                         SegBox* seg, unsigned* done, int n) {
+    __shared__ SegBox sb[kSegTile];
+    const int tid = threadIdx.x;
+    const int l = blockIdx.x * kSegTile + tid;
+    if (l < n) {
+        const int t = sorted_idx[l];
+        SegBox b;
+        for (int k = 0; k < 3; k++) {
+            b.lo[k] = aabb[6 * t + k];
+            b.hi[k] = aabb[6 * t + 3 + k];
+        }
+        BNode& L = nodes[n - 1 + l];
+        for (int k = 0; k < 3; k++) {
+            L.lo[k] = b.lo[k];
+            L.hi[k] = b.hi[k];
+        }
+        L.tri = t;
+        L.left = L.right = -1;
+        L.parent = -1;
+        seg[l] = b;
+        sb[tid] = b;
+    }
+    __syncthreads();
+    // levels 1..10 of this CTA's leaves
+    for (int L = 1; L < kSegTileLevels; L++) {
+        const int span = 1 << L;
+        const int local = tid * span;             // first leaf (CTA-relative) of node tid at level L
+        const int k = (blockIdx.x * kSegTile >> L) + tid;
+        const bool live = local < kSegTile && k < seg_count(n, L);
+        SegBox c;
+        if (live) {
+            c = sb[local];
+            const int right = local + (span >> 1);
+            if (blockIdx.x * kSegTile + right < n) c = seg_union(c, sb[right]);
+        }
+        __syncthreads();
+        if (live) {
+            sb[local] = c;
+            seg[seg_offset(n, L) + k] = c;
+        }
+        __syncthreads();
+    }
+    // the levels above the CTAs, by the last CTA to finish
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) last = atomicAdd(done, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    for (int L = kSegTileLevels; seg_count(n, L - 1) > 1; L++) {
+        const int cnt = seg_count(n, L), below = seg_count(n, L - 1);
+        const int ob = seg_offset(n, L - 1), oc = seg_offset(n, L);
+        for (int k = tid; k < cnt; k += blockDim.x) {
+            SegBox c = seg_load_cg(seg + ob + 2 * k);
+            if (2 * k + 1 < below) c = seg_union(c, seg_load_cg(seg + ob + 2 * k + 1));
+            seg[oc + k] = c;
+        }
+        __threadfence();
+        __syncthreads();
+    }
+    if (tid == 0) *done = 0u;
+}
+
+__global__ void k_lbvh_internal(BNode* nodes, const uint32_t* key, const SegBox* seg, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n - 1) return;
     const int d = (lbvh_delta(key, n, i, i + 1) - lbvh_delta(key, n, i, i - 1)) >= 0 ? 1 : -1;
@@ -702,61 +834,48 @@ __global__ void k_lbvh_internal(BNode* nodes, const uint32_t* key, int n) {
     const int lo = i < j ? i : j, hi = i < j ? j : i;
     const int left = (lo == gamma) ? (n - 1 + gamma) : gamma;
     const int right = (hi == gamma + 1) ? (n - 1 + gamma + 1) : gamma + 1;
-    nodes[i].left = left;
-    nodes[i].right = right;
-    nodes[i].tri = -1;
+    // box of the sorted leaves [lo, hi]: the segment-tree nodes that tile it
+    SegBox box;
+    for (int k = 0; k < 3; k++) {
+        box.lo[k] = 1e300;
+        box.hi[k] = -1e300;
+    }
+    int a = lo, b = hi + 1, L = 0, off = 0;
+    while (a < b) {
+        if (a & 1) box = seg_union(box, seg[off + a++]);
+        if (b & 1) box = seg_union(box, seg[off + --b]);
+        off += seg_count(n, L);
+        a >>= 1;
+        b >>= 1;
+        L++;
+    }
+    BNode& N = nodes[i];
+    for (int k = 0; k < 3; k++) {
+        N.lo[k] = box.lo[k];
+        N.hi[k] = box.hi[k];
+    }
+    N.left = left;
+    N.right = right;
+    N.tri = -1;
     nodes[left].parent = i;
     nodes[right].parent = i;
+    if (i == 0) N.parent = -1;
 }
 
-// Leaves take their triangle's AABB; each leaf thread then climbs, and the
-// second thread to reach a node (atomic counter, no waiting) merges the two
-// children's boxes into it.
-__global__ void k_lbvh_refit(BNode* nodes, const double* aabb, const int* sorted_idx, int* flags, int n) {
-    const int l = blockIdx.x * blockDim.x + threadIdx.x;
-    if (l >= n) return;
-    const int leaf = n - 1 + l;
-    const int t = sorted_idx[l];
-    BNode& L = nodes[leaf];
-    for (int k = 0; k < 3; k++) {
-        L.lo[k] = aabb[6 * t + k];
-        L.hi[k] = aabb[6 * t + 3 + k];
-    }
-    L.tri = t;
-    L.left = L.right = -1;
-    if (n == 1) return;
-    __threadfence();
-    int node = L.parent;
-    while (node >= 0) {
-        const int prev = atomicAdd(&flags[node], 1);
-        if (prev == 0) return;  // first child to arrive stops here
-        __threadfence();
-        BNode& N = nodes[node];
-        const BNode& A = nodes[N.left];
-        const BNode& B = nodes[N.right];
-        for (int k = 0; k < 3; k++) {
-            const double alo = __ldcg(&A.lo[k]), blo = __ldcg(&B.lo[k]);
-            const double ahi = __ldcg(&A.hi[k]), bhi = __ldcg(&B.hi[k]);
-            N.lo[k] = alo < blo ? alo : blo;
-            N.hi[k] = ahi > bhi ? ahi : bhi;
-        }
-        __threadfence();
-        node = N.parent;
-    }
-}
-
-__global__ void k_lbvh_init(BNode* nodes, int* flags, int n) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < 2 * n - 1) nodes[i].parent = -1;
-    if (i < n) flags[i] = 0;
-}
-
-void launch_bvh_build(const double* aabb, BNode* nodes, const uint32_t* morton_sorted,
-                      const int* sorted_idx, int* flags, int ntri, cudaStream_t st) {
+void launch_bvh_build(const double* aabb, BNode* nodes, const uint32_t* morton_sorted, const int* sorted_idx,
+                      void* seg, unsigned* done, int ntri, cudaStream_t st) {
     if (ntri <= 0) return;
-    k_lbvh_init<<<grid_for(2 * ntri), kBlock, 0, st>>>(nodes, flags, ntri);
-    if (ntri > 1) k_lbvh_internal<<<grid_for(ntri - 1), kBlock, 0, st>>>(nodes, morton_sorted, ntri);
-    k_lbvh_refit<<<grid_for(ntri), kBlock, 0, st>>>(nodes, aabb, sorted_idx, flags, ntri);
+    SegBox* sg = static_cast<SegBox*>(seg);
+    k_lbvh_leaves<<<(ntri + kSegTile - 1) / kSegTile, kSegTile, 0, st>>>(nodes, aabb, sorted_idx, sg, done, ntri);
+    if (ntri > 1) k_lbvh_internal<<<grid_for(ntri - 1), kBlock, 0, st>>>(nodes, morton_sorted, sg, ntri);
+}
+
+// the segment tree's nodes: every level up to the root, and at least the
+// levels one CTA writes
+size_t bvh_scratch_bytes(int ntri) {
+    if (ntri <= 0) return 0;
+    const int levels = seg_levels(ntri) > kSegTileLevels ? seg_levels(ntri) : kSegTileLevels;
+    return sizeof(SegBox) * (size_t)seg_offset(ntri, levels);
 }
 
 // FP32 copy of the triangles for the mixed-precision step kernel.

@@ -112,6 +112,73 @@ __device__ __forceinline__ void pair_add(float& hi, float& lo, float d) {
     lo = __fsub_rn(l, __fsub_rn(hi, s));
 }
 
+// a - b as an unevaluated pair (s, e), exactly (Knuth's TwoSum)
+__device__ __forceinline__ void two_diff(float a, float b, float& s, float& e) {
+    s = __fsub_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(-b, bb));
+}
+
+// Geometry of a particle pair from the float-pair positions {hi.xyz, ±r_hi}
+// and {lo.xyz, r_lo}: the relative vector rounded to FP32 (dx, dy, dz), the
+// contact radius Rs = r_i + r_j and num = Rs^2 - |x_i - x_j|^2 to about FP64
+// accuracy.  The high-part differences and the radius sum are split exactly
+// (TwoSum), the squares exactly (FMA), and the large terms cancel in
+// error-free sums, so the overlap num / (Rs + |x_ij|) carries no
+// cancellation error.
+struct PairGeom {
+    float dx, dy, dz, Rs, num;
+};
+__device__ __forceinline__ PairGeom pair_geometry(float4 hi, float4 li, float4 hj, float4 lj) {
+    PairGeom g;
+    float X, Y, Z, eX, eY, eZ;
+    two_diff(hi.x, hj.x, X, eX);
+    two_diff(hi.y, hj.y, Y, eY);
+    two_diff(hi.z, hj.z, Z, eZ);
+    eX = __fadd_rn(eX, __fsub_rn(li.x, lj.x));
+    eY = __fadd_rn(eY, __fsub_rn(li.y, lj.y));
+    eZ = __fadd_rn(eZ, __fsub_rn(li.z, lj.z));
+    float S, eS;
+    two_diff(fabsf(hi.w), -fabsf(hj.w), S, eS);
+    const float Rl = __fadd_rn(eS, __fadd_rn(li.w, lj.w));
+    const float p0 = __fmul_rn(S, S), e0 = __fmaf_rn(S, S, -p0);
+    const float p1 = __fmul_rn(X, X), e1 = __fmaf_rn(X, X, -p1);
+    const float p2 = __fmul_rn(Y, Y), e2 = __fmaf_rn(Y, Y, -p2);
+    const float p3 = __fmul_rn(Z, Z), e3 = __fmaf_rn(Z, Z, -p3);
+    float a, t1, t2, t3;
+    two_diff(p0, p1, a, t1);
+    two_diff(a, p2, a, t2);
+    two_diff(a, p3, a, t3);
+    const float small = __fadd_rn(__fadd_rn(__fadd_rn(t1, t2), t3), __fsub_rn(__fsub_rn(__fsub_rn(e0, e1), e2), e3));
+    const float cross = __fsub_rn(__fmul_rn(S, Rl), __fadd_rn(__fadd_rn(__fmul_rn(X, eX), __fmul_rn(Y, eY)), __fmul_rn(Z, eZ)));
+    g.num = __fadd_rn(a, __fadd_rn(small, __fmul_rn(2.f, cross)));
+    g.dx = __fadd_rn(X, eX);
+    g.dy = __fadd_rn(Y, eY);
+    g.dz = __fadd_rn(Z, eZ);
+    g.Rs = __fadd_rn(S, Rl);
+    return g;
+}
+
+// First contact test on the high parts alone (one gather per candidate):
+// 1 surely in contact, 0 surely not, -1 undecided (within `delta`, the bound
+// on what the low parts can move the distance, of touching).
+__device__ __forceinline__ int contact_hint(float4 hi, float4 hj, float delta) {
+    if (!(hj.w > 0.f)) return 0;  // partner inactive or leaving the box
+    const float dx = hi.x - hj.x, dy = hi.y - hj.y, dz = hi.z - hj.z;
+    const float Rs = hi.w + hj.w;
+    const float d2 = dx * dx + dy * dy + dz * dz;
+    const float Rin = Rs - delta, Rout = Rs + delta;
+    if (Rin > 0.f && d2 < Rin * Rin * 0.9999981f) return 1;
+    if (d2 > Rout * Rout * 1.0000019f) return 0;
+    return -1;
+}
+
+// The exact contact test (pair_geometry's num > 0) for the few candidates the
+// high parts leave undecided; kept out of line so the scan loop stays small.
+__device__ __noinline__ bool exact_contact(float4 hi, float4 li, float4 hj, float4 lj) {
+    return pair_geometry(hi, li, hj, lj).num > 0.f;
+}
+
 }  // namespace
 
 // End of a step kernel: refresh vote, error bits, and in the last CTA the
@@ -165,15 +232,17 @@ struct Force6 {
 // calc_tangential_force, cpu_dem.cu:953, :783, or the Hertz-Mindlin law),
 // with the spring history (sp, cp) of the contact updated in place.
 template <int MODEL>
-__device__ __forceinline__ Force6 pair_force(const View<Mixed>& v, float dx, float dy, float dz, float ri, float rj,
+__device__ __forceinline__ Force6 pair_force(const View<Mixed>& v, const PairGeom& g, float ri, float rj,
                                              float4 vi, float4 wi, float4 vj, float4 wj, float invmi, const Mat& m,
                                              Vec3<float>& sp, Vec3<float>& cp) {
     using R = float;
+    const R dx = g.dx, dy = g.dy, dz = g.dz;
     const R distsq = dx * dx + dy * dy + dz * dz;
-    const R Rs = ri + rj;
+    const R Rs = g.Rs;
     const R dist = sqrtf(distsq);
     const R inv = 1.f / dist;
-    const R delMag = Rs - dist;
+    // the overlap Rs - dist without its cancellation: (Rs^2 - d^2) / (Rs + d)
+    const R delMag = g.num / (Rs + dist);
     const R nx = dx * inv, ny = dy * inv, nz = dz * inv;
     const R vrx = vi.x - vj.x, vry = vi.y - vj.y, vrz = vi.z - vj.z;
     const R vdn = vrx * nx + vry * ny + vrz * nz;
@@ -359,10 +428,10 @@ __device__ __forceinline__ void wall_forces(const View<Mixed>& v, const PBank<Mi
 // Inactive particle, or one that left the box last step (status 2): frozen
 // from now on.
 __device__ __forceinline__ void freeze_one(const View<Mixed>& v, const SBank<Mixed>& B, int i, const Own& o) {
-    float4 li = o.li, wi = o.wi;
-    B.posh[i] = o.hi;
-    li.w = 0.f;
-    B.posl[i] = li;
+    float4 hi = o.hi, wi = o.wi;
+    hi.w = -fabsf(hi.w);
+    B.posh[i] = hi;
+    B.posl[i] = o.li;
     B.vel[i] = o.vi;
     B.vell[i] = o.vl;
     B.rotl[i] = o.wl;
@@ -421,7 +490,7 @@ __device__ __forceinline__ void integrate_one(const View<Mixed>& v, const SBank<
         err |= 0x20u;
         status = 2.f;
     }
-    nl.w = status;
+    nh.w = status == 1.f ? fabsf(o.hi.w) : -fabsf(o.hi.w);
     B.posh[i] = nh;
     B.posl[i] = nl;
     B.vel[i] = make_float4(nvx, nvy, nvz, invmi);
@@ -466,23 +535,16 @@ __device__ __forceinline__ void step_one(const View<Mixed>& v, const SBank<Mixed
             const int k = k0 + q;
             jj[q] = k < nn ? (k < nei_s_rows ? nei_s[k * 32] : __ldg(&nei[(size_t)k * n + i])) : -1;
         }
-        float4 hj[4], lj[4];
+        float4 hj[4];
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
-            if (jj[q] >= 0) {
-                hj[q] = __ldg(&Aposh[jj[q]]);
-                lj[q] = __ldg(&Aposl[jj[q]]);
-            }
-        }
+        for (int q = 0; q < 4; q++)
+            if (jj[q] >= 0) hj[q] = __ldg(&Aposh[jj[q]]);
         unsigned hit = 0u;
 #pragma unroll
         for (int q = 0; q < 4; q++) {
-            if (jj[q] < 0 || lj[q].w != 1.f) continue;
-            const R dx = (hi.x - hj[q].x) + (li.x - lj[q].x);
-            const R dy = (hi.y - hj[q].y) + (li.y - lj[q].y);
-            const R dz = (hi.z - hj[q].z) + (li.z - lj[q].z);
-            const R Rs = ri + hj[q].w;
-            if (dx * dx + dy * dy + dz * dz < Rs * Rs) hit |= 1u << q;
+            if (jj[q] < 0) continue;
+            const int h = contact_hint(hi, hj[q], v.nb_delta);
+            if (h > 0 || (h < 0 && exact_contact(hi, li, hj[q], __ldg(&Aposl[jj[q]])))) hit |= 1u << q;
         }
         while (hit) {
             const int q = __ffs(hit) - 1;
@@ -490,9 +552,6 @@ __device__ __forceinline__ void step_one(const View<Mixed>& v, const SBank<Mixed
             const int k = k0 + q;
             const int j = k < nei_s_rows ? nei_s[k * 32] : __ldg(&nei[(size_t)k * n + i]);
             const float4 hjq = __ldg(&Aposh[j]), ljq = __ldg(&Aposl[j]);
-            const R dx = (hi.x - hjq.x) + (li.x - ljq.x);
-            const R dy = (hi.y - hjq.y) + (li.y - ljq.y);
-            const R dz = (hi.z - hjq.z) + (li.z - ljq.z);
             bool fresh;
             const int slot = find_slot<T>(P.hid, n, i, nc, j, v.hist_cap, fresh);
             if (slot < 0) {
@@ -510,7 +569,7 @@ __device__ __forceinline__ void step_one(const View<Mixed>& v, const SBank<Mixed
                 cp.x = P.cx[h]; cp.y = P.cy[h]; cp.z = P.cz[h];
             }
             touched |= 1ull << slot;
-            const Force6 G = pair_force<MODEL>(v, dx, dy, dz, ri, hjq.w, o.vi, o.wi, __ldg(&Avel[j]), __ldg(&Arot[j]),
+            const Force6 G = pair_force<MODEL>(v, pair_geometry(hi, li, hjq, ljq), ri, hjq.w, o.vi, o.wi, __ldg(&Avel[j]), __ldg(&Arot[j]),
                                                invmi, mt, sp, cp);
             F.fx += G.fx; F.fy += G.fy; F.fz += G.fz;
             F.mx += G.mx; F.my += G.my; F.mz += G.mz;
@@ -879,6 +938,7 @@ __global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<
         unsigned long long hit_lo = 0ull, hit_hi = 0ull;
         {
             const float4 hi = S.posh[lane], li = S.posl[lane];
+            const float delta = v.nb_delta;
             for (int k0 = 0; k0 < nn; k0 += 4) {
                 int jj[4];
 #pragma unroll
@@ -886,23 +946,16 @@ __global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<
                     const int k = k0 + q;
                     jj[q] = k < nn ? (k < nei_rows ? nei_s[k * 32] : __ldg(&nei[(size_t)k * n + i])) : -1;
                 }
-                float4 hj[4], lj[4];
+                float4 hj[4];
 #pragma unroll
-                for (int q = 0; q < 4; q++) {
-                    if (jj[q] >= 0) {
-                        hj[q] = __ldg(&Aposh[jj[q]]);
-                        lj[q] = __ldg(&Aposl[jj[q]]);
-                    }
-                }
+                for (int q = 0; q < 4; q++)
+                    if (jj[q] >= 0) hj[q] = __ldg(&Aposh[jj[q]]);
                 unsigned hit = 0u;
 #pragma unroll
                 for (int q = 0; q < 4; q++) {
-                    if (jj[q] < 0 || lj[q].w != 1.f) continue;
-                    const R dx = (hi.x - hj[q].x) + (li.x - lj[q].x);
-                    const R dy = (hi.y - hj[q].y) + (li.y - lj[q].y);
-                    const R dz = (hi.z - hj[q].z) + (li.z - lj[q].z);
-                    const R Rs = hi.w + hj[q].w;
-                    if (dx * dx + dy * dy + dz * dz < Rs * Rs) hit |= 1u << q;
+                    if (jj[q] < 0) continue;
+                    const int h = contact_hint(hi, hj[q], delta);
+                    if (h > 0 || (h < 0 && exact_contact(hi, li, hj[q], __ldg(&Aposl[jj[q]])))) hit |= 1u << q;
                 }
                 if (k0 < 64)
                     hit_lo |= (unsigned long long)hit << k0;
@@ -966,11 +1019,9 @@ __global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<
                     sp.x = P.hx[h]; sp.y = P.hy[h]; sp.z = P.hz[h];
                     cp.x = P.cx[h]; cp.y = P.cy[h]; cp.z = P.cz[h];
                 }
-                const R dx = (hiw.x - hjq.x) + (liw.x - ljq.x);
-                const R dy = (hiw.y - hjq.y) + (liw.y - ljq.y);
-                const R dz = (hiw.z - hjq.z) + (liw.z - ljq.z);
                 const Mat mo = own_material<MODEL>(P, iow, hiw.w, viw.w);
-                const Force6 G = pair_force<MODEL>(v, dx, dy, dz, hiw.w, hjq.w, viw, wiw, vj, wj, viw.w, mo, sp, cp);
+                const Force6 G = pair_force<MODEL>(v, pair_geometry(hiw, liw, hjq, ljq), hiw.w, hjq.w, viw, wiw, vj, wj,
+                                                   viw.w, mo, sp, cp);
                 P.hx[h] = sp.x; P.hy[h] = sp.y; P.hz[h] = sp.z;
                 P.cx[h] = cp.x; P.cy[h] = cp.y; P.cz[h] = cp.z;
                 que->f[r][0][ow] = G.fx;
