@@ -114,7 +114,23 @@ def dist_init():
     return None, 0, 1
 
 
-def _time_steps(E, steps, warmup, stream, clk=None):
+def _nvtx(name=None):
+    """Open an NVTX range (name) or close the innermost one (None); a no-op
+    where NVTX is unavailable."""
+    import torch
+    try:
+        if name is None:
+            torch.cuda.nvtx.range_pop()
+        else:
+            torch.cuda.nvtx.range_push(name)
+    except Exception:  # noqa: BLE001
+        pass
+
+
+def _time_steps(E, steps, warmup, stream, clk=None, tag="timed"):
+    """Warm-up steps, then `steps` steps between two CUDA events on the
+    engine's stream.  The timed steps sit in an NVTX range named `tag`, so a
+    profiler can be restricted to them (ncu --nvtx --nvtx-include "timed/")."""
     import torch
     E.step(warmup)
     E.sync()
@@ -124,10 +140,12 @@ def _time_steps(E, steps, warmup, stream, clk=None):
     torch.cuda.synchronize()
     if clk is not None:
         clk.__enter__()
+    _nvtx(tag)
     start.record(stream)
     E.step(steps)
     stop.record(stream)
     stop.synchronize()
+    _nvtx()
     torch.cuda.synchronize()
     if clk is not None:
         clk.__exit__()
@@ -172,7 +190,9 @@ def run_engine(args):
     n_act = 0.5 * (st0["n_active"] + st1["n_active"])
     value = n_act * args.steps * ws / (ms / 1e3)
     # dominant kernel: the step kernel alone, CUDA events on the engine stream
+    _nvtx("profile")
     k_ms = E.profile_step(args.profile_iters)
+    _nvtx()
     stk = E.stats()
     mixed = args.precision == "mixed"
     bytes_launch = algorithmic_bytes(stk, stk["n_active"], s=4 if mixed else 8, s_h=8)
@@ -184,7 +204,8 @@ def run_engine(args):
     if not args.bvh_once:
         # context: the same steps with the LBVH of the static mesh built once
         E1 = engine.Engine(sc, precision=args.precision, **dict(kw, bvh_every_step=False))
-        ms1, a0, a1 = _time_steps(E1, max(10, args.steps // 4), args.warmup, torch.cuda.ExternalStream(E1.stream()))
+        ms1, a0, a1 = _time_steps(E1, max(10, args.steps // 4), args.warmup, torch.cuda.ExternalStream(E1.stream()),
+                                  tag="timed_lbvh_once")
         E1.close()
         extra["value_lbvh_built_once"] = 0.5 * (a0["n_active"] + a1["n_active"]) * max(10, args.steps // 4) / (ms1 / 1e3)
     if mixed and not args.no_fp64:
@@ -192,7 +213,7 @@ def run_engine(args):
         F = engine.Engine(sc, precision="fp64", **kw)
         fstream = torch.cuda.ExternalStream(F.stream())
         fsteps = max(10, args.steps // 4)
-        fms, f0, f1 = _time_steps(F, fsteps, args.warmup, fstream)
+        fms, f0, f1 = _time_steps(F, fsteps, args.warmup, fstream, tag="timed_fp64")
         fval = 0.5 * (f0["n_active"] + f1["n_active"]) * fsteps / (fms / 1e3)
         F.close()
         extra.update({"fp64_value": fval, "fp64_steps": fsteps, "mixed_over_fp64": value / fval})
@@ -334,6 +355,58 @@ def run_reference(args):
     print(json.dumps(out))
 
 
+def run_batched(args):
+    """Batched ensemble: 256 independent scenes of uneven size packed into one
+    engine (one persistent step launch per step, CUDA graphs), against the
+    same scenes stepped one by one, each in its own engine.  Both arms run the
+    mixed-precision Hertz-Mindlin step with each scene's own friction and
+    restitution."""
+    import torch
+    from gpudem_gb300 import engine, scenes
+    dist, rank, ws = dist_init()
+    if rank != 0:
+        return
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    scs = scenes.config4_batched(n_scenes=args.n_scenes)
+    packed, offs, starts = scenes.pack_scenes(scs)
+    kw = dict(model="hertz_mindlin", steps_per_graph=8)
+    E = engine.Engine(packed, precision=args.precision, **kw)
+    stream = torch.cuda.ExternalStream(E.stream())
+    out_dir = os.path.join(ROOT, "gpurun_out") if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp"
+    clk = Clocks(os.path.join(out_dir, "clocks_batched.csv"))
+    ms, st0, st1 = _time_steps(E, args.steps, args.warmup, stream, clk)
+    n_act = 0.5 * (st0["n_active"] + st1["n_active"])
+    value = n_act * args.steps / (ms / 1e3)
+    reb = int(st1["rebuilds"] - st0["rebuilds"])
+    E.close()
+    # one by one: each scene in its own engine, timed steps only
+    seq_steps = max(10, args.seq_steps)
+    seq_ms = 0.0
+    seq_ps = 0.0
+    for sc in scs:
+        Es = engine.Engine(sc, precision=args.precision, **kw)
+        sst = torch.cuda.ExternalStream(Es.stream())
+        t_ms, a0, a1 = _time_steps(Es, seq_steps, 3, sst)
+        seq_ms += t_ms
+        seq_ps += 0.5 * (a0["n_active"] + a1["n_active"]) * seq_steps
+        Es.close()
+    seq_value = seq_ps / (seq_ms / 1e3)
+    out = {"metric": "particle-steps/s, 256 uneven scenes in one launch (batched) vs one by one",
+           "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32" if args.precision == "mixed" else "f64",
+           "data": "synthetic (256 seeded box-drop scenes, config 4 of the benchmark set)",
+           "config": {"workload": f"{len(scs)} box-drop scenes, {packed.n} spheres in all (per scene "
+                                  f"{min(sc.n for sc in scs)}..{max(sc.n for sc in scs)}), "
+                                  f"{packed.tris.shape[0]} triangles in all (per scene "
+                                  f"{min(sc.tris.shape[0] for sc in scs)}..{max(sc.tris.shape[0] for sc in scs)}), "
+                                  f"hertz_mindlin, per-scene mu and e, {args.precision}",
+                      "one_by_one_value": seq_value, "one_by_one_steps_per_scene": seq_steps,
+                      "batched_over_one_by_one": value / seq_value, "rebuilds_in_timed_region": reb},
+           "clocks": clk.summary(), "gpu_launches": args.steps + reb * 19}
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -354,7 +427,9 @@ def main():
     ap.add_argument("--v-sigma", type=float, default=0.5)
     ap.add_argument("--profile-iters", type=int, default=10)
     ap.add_argument("--e2e-steps", type=int, default=500)
-    ap.add_argument("--workload", default="poured", choices=["poured", "lattice"])
+    ap.add_argument("--workload", default="poured", choices=["poured", "lattice", "batched"])
+    ap.add_argument("--n-scenes", type=int, default=256)
+    ap.add_argument("--seq-steps", type=int, default=200)
     ap.add_argument("--bvh-once", action="store_true",
                     help="build the static mesh's LBVH once instead of in every step")
     ap.add_argument("--settle-steps", type=int, default=12000)
@@ -364,6 +439,8 @@ def main():
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batched":
+        run_batched(args)
     else:
         run_engine(args)
 

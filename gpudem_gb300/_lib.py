@@ -20,7 +20,7 @@ EXPORTED = [
     "gdem_create", "gdem_destroy", "gdem_last_error", "gdem_set_mesh", "gdem_import_particles",
     "gdem_step", "gdem_synchronize", "gdem_export_particles", "gdem_stats_get", "gdem_rebuild",
     "gdem_export_lists", "gdem_morton_keys", "gdem_export_cells", "gdem_sort_keys",
-    "gdem_sort_keys_noalloc", "gdem_set_mesh_indexed",
+    "gdem_sort_keys_noalloc", "gdem_set_mesh_indexed", "gdem_set_particle_materials",
     "gdem_dist_triangle", "gdem_export_mesh", "gdem_get_stream", "gdem_profile_step",
     "gdem_export_positions",
 ]
@@ -114,6 +114,7 @@ def load(build_if_missing: bool = False):
     L.gdem_sort_keys.argtypes = [vp, C.c_int, vp, vp]
     L.gdem_sort_keys_noalloc.argtypes = [vp, C.c_int, vp, vp, vp]
     L.gdem_set_mesh_indexed.argtypes = [vp, C.POINTER(MeshArrays)]
+    L.gdem_set_particle_materials.argtypes = [vp, vp, vp]
     L.gdem_dist_triangle.argtypes = [vp, vp, vp, vp, C.c_int, vp, vp]
     L.gdem_export_mesh.argtypes = [vp, vp, vp, vp, vp, vp]
     L.gdem_get_stream.argtypes = [vp, C.POINTER(vp)]

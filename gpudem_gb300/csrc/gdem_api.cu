@@ -84,6 +84,7 @@ struct EngineBase {
     virtual int cells(uint32_t* ks, int* order, int* pNum, int* pStart, int* pList, int* ncell) = 0;
     virtual int stats(gdem_stats* s) = 0;
     virtual int profile(int iters, float* ms) = 0;
+    virtual int set_materials(const double* mu, const double* restitution) = 0;
     virtual void set_mesh(const MeshData& m) = 0;
     virtual unsigned error_word() = 0;
     std::string err;
@@ -319,6 +320,7 @@ struct Impl : EngineBase {
     int import_(const gdem_particles* p) override {
         CKE(cudaStreamSynchronize(st));
         destroy_graphs();
+        v.per_particle_mat = 0;
         const int H = v.hist_cap, HW = v.histw_cap;
         std::vector<double4_32a> pos(n);
         std::vector<V4> vel(n), rot(n), mat(n);
@@ -734,6 +736,33 @@ struct Impl : EngineBase {
         return GDEM_OK;
     }
 
+    // Hertz-Mindlin friction and damping per particle (pId order), written
+    // into the material records of the current property bank.
+    int set_materials(const double* mu, const double* restitution) override {
+        if (d.model != GDEM_HERTZ_MINDLIN)
+            return failv(err, GDEM_ERR_STATE, "per-particle materials need the Hertz-Mindlin model");
+        Ctl c;
+        std::vector<int> pid;
+        int rc = current(c, pid);
+        if (rc) return rc;
+        std::vector<V4> mat;
+        if ((rc = dl(mat, v.P[c.p].mat, n))) return rc;
+        for (int i = 0; i < n; i++) {
+            const int q = pid[i];
+            const double e = restitution[q];
+            if (!(e > 0. && e <= 1.) || !(mu[q] >= 0.))
+                return failv(err, GDEM_ERR_ARG, "restitution must be in (0, 1] and friction >= 0");
+            const double le = log(e);
+            const double beta = le / sqrt(le * le + M_PI * M_PI);
+            mat[i].x = (R)mu[q];
+            mat[i].y = (R)(-2. * sqrt(5. / 6.) * beta);
+        }
+        CKE(cudaMemcpy(v.P[c.p].mat, mat.data(), sizeof(V4) * n, cudaMemcpyHostToDevice));
+        destroy_graphs();
+        v.per_particle_mat = 1;
+        return GDEM_OK;
+    }
+
     int profile(int iters, float* avg_ms) override {
         // groups of kProfileBurst launches back to back between two events;
         // the device-gated rebuild runs after each group
@@ -1126,6 +1155,12 @@ int gdem_stats_get(gdem_handle* h, gdem_stats* s) {
     if (!h || !s) return GDEM_ERR_ARG;
     if (!h->eng->imported) return fail(h, GDEM_ERR_STATE, "stats before import");
     return pass(h, h->eng->stats(s));
+}
+
+int gdem_set_particle_materials(gdem_handle* h, const double* mu, const double* restitution) {
+    if (!h || !mu || !restitution) return GDEM_ERR_ARG;
+    if (!h->eng->imported) return fail(h, GDEM_ERR_STATE, "materials before import");
+    return pass(h, h->eng->set_materials(mu, restitution));
 }
 
 int gdem_get_stream(gdem_handle* h, void** stream) {

@@ -102,7 +102,8 @@ struct SBank {
 };
 
 // material record: linear model {k, etaconst, sqrt(m), 1/I};
-// Hertz-Mindlin {0, 0, sqrt(m), 1/I}
+// Hertz-Mindlin {k, etaconst, sqrt(m), 1/I}, or {mu, damping -2 sqrt(5/6) beta,
+// sqrt(m), 1/I} once per-particle materials are set (gdem_set_particle_materials)
 template <class T>
 struct PBank {
     typename T::v4* mat;
@@ -174,6 +175,7 @@ struct View {
     double skin, thresh_sq;
     float boxf[6];                   // mixed mode: box rounded outwards to FP32
     float nb_delta;                  // bound on |d_fp32 - d| of the list prefilter (m)
+    int per_particle_mat;            // Hertz-Mindlin: mu and damping from mat.x, mat.y of each particle
     // the scalars above rounded to FP32 once, for the mixed step
     float dtf, gxf, gyf, gzf, thresh_sqf;
     float muf, kn_cf, sn_cf, kt_cf, damp_cf, mu_rollf;

@@ -162,7 +162,12 @@ __global__ void __launch_bounds__(kBlock) k_step(View<T> v, cudaGraphConditional
             const R ri = (R)pi.w;
             const R invmi = vi.w;
             const R ki = mi.x, etai = mi.y, sqrtmi = mi.z, invmoi = mi.w;
-            const R dt = (R)v.dt, mu = (R)v.mat.mu;
+            const R dt = (R)v.dt;
+            // Hertz-Mindlin per-particle materials: both particles of a contact
+            // belong to the same scene, so the particle's own values serve
+            const bool pm = MODEL == 1 && v.per_particle_mat;
+            const R mu = pm ? (R)mi.x : (R)v.mat.mu;
+            const R damp_c = pm ? (R)mi.y : (R)v.mat.damp_c;
             R fx = R(0.), fy = R(0.), fz = R(0.);
             R mx = R(0.), my = R(0.), mz = R(0.);
 
@@ -206,13 +211,13 @@ __global__ void __launch_bounds__(kBlock) k_step(View<T> v, cudaGraphConditional
                     const R mstar = R(1.) / (invmi + vj.w);
                     const R sqrtRd = sqrt_<R>(Rstar * delMag);
                     const R fel = (R)v.mat.kn_c * sqrtRd * delMag;
-                    const R gn = (R)v.mat.damp_c * sqrt_<R>((R)v.mat.sn_c * sqrtRd * mstar);
+                    const R gn = damp_c * sqrt_<R>((R)v.mat.sn_c * sqrtRd * mstar);
                     const R fnm = fel - gn * vdn;
                     fnx = fnm * nx;
                     fny = fnm * ny;
                     fnz = fnm * nz;
                     kt = (R)v.mat.kt_c * sqrtRd;
-                    gt = (R)v.mat.damp_c * sqrt_<R>(kt * mstar);
+                    gt = damp_c * sqrt_<R>(kt * mstar);
                 }
                 const R ax_ = ri * wi.x + rj * wj.x;
                 const R ay_ = ri * wi.y + rj * wj.y;
@@ -326,13 +331,13 @@ __global__ void __launch_bounds__(kBlock) k_step(View<T> v, cudaGraphConditional
                     const R mstar = R(1.) / invmi;
                     const R sqrtRd = sqrt_<R>(ri * delmag);
                     const R fel = (R)v.mat.kn_c * sqrtRd * delmag;
-                    const R gn = (R)v.mat.damp_c * sqrt_<R>((R)v.mat.sn_c * sqrtRd * mstar);
+                    const R gn = damp_c * sqrt_<R>((R)v.mat.sn_c * sqrtRd * mstar);
                     const R fnm = fel - gn * vdn;
                     fnx = fnm * nx;
                     fny = fnm * ny;
                     fnz = fnm * nz;
                     kt = (R)v.mat.kt_c * sqrtRd;
-                    gt = (R)v.mat.damp_c * sqrt_<R>(kt * mstar);
+                    gt = damp_c * sqrt_<R>(kt * mstar);
                 }
                 const R ax_ = ri * wi.x, ay_ = ri * wi.y, az_ = ri * wi.z;
                 const R crx = ay_ * nz - az_ * ny;

@@ -206,20 +206,33 @@ struct Own {
     int nn, nw, nc, ncw;
 };
 
-// Per-particle contact constants.
+// Per-particle contact constants (Hertz-Mindlin: the scene's friction and
+// damping, per particle when the engine has per-particle materials).
 struct Mat {
     float ki, etai, sqrtmi, invmoi;
+    float mu, damp;
 };
 
 template <int MODEL>
-__device__ __forceinline__ Mat own_material(const PBank<Mixed>& P, int i, float ri, float invmi) {
+__device__ __forceinline__ Mat own_material(const View<Mixed>& v, const PBank<Mixed>& P, int i, float ri,
+                                            float invmi) {
     Mat m;
     if (MODEL == 0) {
         const float4 mi = __ldg(&P.mat[i]);
         m.ki = mi.x; m.etai = mi.y; m.sqrtmi = mi.z; m.invmoi = mi.w;
+        m.mu = v.muf;
+        m.damp = 0.f;
     } else {
         m.ki = m.etai = m.sqrtmi = 0.f;
         m.invmoi = 2.5f * invmi / (ri * ri);  // 1 / (2/5 m r^2)
+        if (v.per_particle_mat) {
+            const float4 mi = __ldg(&P.mat[i]);
+            m.mu = mi.x;
+            m.damp = mi.y;
+        } else {
+            m.mu = v.muf;
+            m.damp = v.damp_cf;
+        }
     }
     return m;
 }
@@ -262,13 +275,13 @@ __device__ __forceinline__ Force6 pair_force(const View<Mixed>& v, const PairGeo
         const R mstar = 1.f / (invmi + vj.w);
         const R sqrtRd = sqrtf(Rstar * delMag);
         const R fel = v.kn_cf * sqrtRd * delMag;
-        const R gn = v.damp_cf * sqrtf(v.sn_cf * sqrtRd * mstar);
+        const R gn = m.damp * sqrtf(v.sn_cf * sqrtRd * mstar);
         const R fnm = fel - gn * vdn;
         fnx = fnm * nx;
         fny = fnm * ny;
         fnz = fnm * nz;
         kt = v.kt_cf * sqrtRd;
-        gt = v.damp_cf * sqrtf(kt * mstar);
+        gt = m.damp * sqrtf(kt * mstar);
     }
     const R ax_ = ri * wi.x + rj * wj.x;
     const R ay_ = ri * wi.y + rj * wj.y;
@@ -278,7 +291,7 @@ __device__ __forceinline__ Force6 pair_force(const View<Mixed>& v, const PairGeo
     const R vtz = (vrz - vnz) + (ax_ * ny - ay_ * nx);
     Vec3<R> ft;
     const R fnsq = fnx * fnx + fny * fny + fnz * fnz;
-    tangential<Mixed>(nx, ny, nz, fnsq, vtx, vty, vtz, gt, kt, v.muf, v.dtf, sp, cp, ft);
+    tangential<Mixed>(nx, ny, nz, fnsq, vtx, vty, vtz, gt, kt, m.mu, v.dtf, sp, cp, ft);
     Force6 F;
     F.fx = fnx + ft.x;
     F.fy = fny + ft.y;
@@ -368,13 +381,13 @@ __device__ __forceinline__ void wall_forces(const View<Mixed>& v, const PBank<Mi
             const R mstar = 1.f / invmi;
             const R sqrtRd = sqrtf(ri * delmag);
             const R fel = v.kn_cf * sqrtRd * delmag;
-            const R gn = v.damp_cf * sqrtf(v.sn_cf * sqrtRd * mstar);
+            const R gn = mt.damp * sqrtf(v.sn_cf * sqrtRd * mstar);
             const R fnm = fel - gn * vdn;
             fnx = fnm * nx;
             fny = fnm * ny;
             fnz = fnm * nz;
             kt = v.kt_cf * sqrtRd;
-            gt = v.damp_cf * sqrtf(kt * mstar);
+            gt = mt.damp * sqrtf(kt * mstar);
         }
         const R ax_ = ri * wi.x, ay_ = ri * wi.y, az_ = ri * wi.z;
         const R vtx = (vi.x - vnx) + (ay_ * nz - az_ * ny);
@@ -402,7 +415,7 @@ __device__ __forceinline__ void wall_forces(const View<Mixed>& v, const PBank<Mi
         wtouched |= 1ull << slot;
         Vec3<R> ft;
         const R fnsq = fnx * fnx + fny * fny + fnz * fnz;
-        tangential<T>(nx, ny, nz, fnsq, vtx, vty, vtz, gt, kt, v.muf, v.dtf, sp, cp, ft);
+        tangential<T>(nx, ny, nz, fnsq, vtx, vty, vtz, gt, kt, mt.mu, v.dtf, sp, cp, ft);
         F.fx += ft.x;
         F.fy += ft.y;
         F.fz += ft.z;
@@ -523,7 +536,7 @@ __device__ __forceinline__ void step_one(const View<Mixed>& v, const SBank<Mixed
     const float4 hi = o.hi, li = o.li;
     const R ri = hi.w;
     const R invmi = o.vi.w;
-    const Mat mt = own_material<MODEL>(P, i, ri, invmi);
+    const Mat mt = own_material<MODEL>(v, P, i, ri, invmi);
     Force6 F = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     int nc = o.nc;
     const int nn = o.nn;
@@ -1019,7 +1032,7 @@ __global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<
                     sp.x = P.hx[h]; sp.y = P.hy[h]; sp.z = P.hz[h];
                     cp.x = P.cx[h]; cp.y = P.cy[h]; cp.z = P.cz[h];
                 }
-                const Mat mo = own_material<MODEL>(P, iow, hiw.w, viw.w);
+                const Mat mo = own_material<MODEL>(v, P, iow, hiw.w, viw.w);
                 const Force6 G = pair_force<MODEL>(v, pair_geometry(hiw, liw, hjq, ljq), hiw.w, hjq.w, viw, wiw, vj, wj,
                                                    viw.w, mo, sp, cp);
                 P.hx[h] = sp.x; P.hy[h] = sp.y; P.hz[h] = sp.z;
@@ -1052,7 +1065,7 @@ __global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<
             o.li = S.posl[lane];
             o.vi = S.vel[lane];
             const R invmi = o.vi.w;
-            const Mat mt = own_material<MODEL>(P, i, o.hi.w, invmi);
+            const Mat mt = own_material<MODEL>(v, P, i, o.hi.w, invmi);
             wall_forces<MODEL, WCAP>(v, P, i, S.nneiw[lane], S.ncw[lane], o.hi, o.li, o.vi, o.wi, invmi, mt, F, err);
             o.vl = __ldg(&A.vell[i]);
             o.wl = __ldg(&A.rotl[i]);

@@ -89,6 +89,8 @@ class Engine:
         if scene.tris is not None and len(scene.tris):
             self.set_mesh(scene.tris)
         self.import_particles(scene, history=scene.history, hist_stride=scene.hist_stride)
+        if scene.mu_p is not None:
+            self.set_particle_materials(scene.mu_p, scene.e_p)
 
     # ------------------------------------------------------------------ setup
     def _check(self, rc, what):
@@ -141,6 +143,13 @@ class Engine:
                 self._keep.append(a)
                 setattr(p, nm, _ptr(a, C.c_int if a.dtype == np.int32 else C.c_double))
         self._check(self.L.gdem_import_particles(self.h, C.byref(p)), "gdem_import_particles")
+
+    def set_particle_materials(self, mu, restitution):
+        """Hertz-Mindlin friction and restitution per particle (pId order)."""
+        mu = np.ascontiguousarray(mu, np.float64)
+        e = np.ascontiguousarray(restitution, np.float64)
+        assert mu.size == self.n and e.size == self.n
+        self._check(self.L.gdem_set_particle_materials(self.h, _vp(mu), _vp(e)), "gdem_set_particle_materials")
 
     # ------------------------------------------------------------------ stepping
     def step(self, nsteps=1):

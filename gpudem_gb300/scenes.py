@@ -274,6 +274,9 @@ class Scene:
     history: dict | None = None
     hist_stride: int = 0
     active: np.ndarray | None = None   # (N,) isActive; None: all active
+    # per-particle Hertz-Mindlin friction and restitution (packed scenes)
+    mu_p: np.ndarray | None = None
+    e_p: np.ndarray | None = None
 
     @property
     def n(self) -> int:
@@ -439,3 +442,99 @@ def settle_scene(sc: Scene, steps=10_000, dt=2e-5, e=0.1, precision="mixed", his
     return replace(sc, x=st["x"].reshape(-1, 3), v=st["v"].reshape(-1, 3), w=st["angv"].reshape(-1, 3),
                    history=hist, hist_stride=hist_stride, active=act,
                    name=sc.name + f"-settled{steps}")
+
+
+def box_mesh_grid(half=0.1, k=1, center=(0.0, 0.0, 0.0)) -> np.ndarray:
+    """Closed axis-aligned cube of side 2*half with every face split into k x k
+    quads: 12 k^2 triangles."""
+    c = np.asarray(center, dtype=np.float64)
+    h = float(half)
+    faces = [  # corner, u axis, v axis (outward normal = u x v)
+        ((1, -1, -1), (0, 2, 0), (0, 0, 2)), ((-1, -1, 1), (2, 0, 0), (0, 2, 0)),
+        ((-1, -1, -1), (0, 0, 2), (0, 2, 0)), ((-1, -1, -1), (0, 2, 0), (2, 0, 0)),
+        ((-1, 1, -1), (0, 0, 2), (2, 0, 0)), ((-1, -1, -1), (2, 0, 0), (0, 0, 2)),
+    ]
+    tris = []
+    for o, u, w in faces:
+        o, u, w = (np.asarray(a, dtype=np.float64) for a in (o, u, w))
+        for i in range(k):
+            for j in range(k):
+                p = lambda a, b: c + h * (o + u * (a / k) + w * (b / k))
+                tris += _quad(p(i, j), p(i + 1, j), p(i + 1, j + 1), p(i, j + 1))
+    return np.asarray(tris, dtype=np.float64)
+
+
+def config4_batched(n_scenes=256, seed=4, n_min=1000, n_max=50_000) -> list:
+    """Batched ensemble: `n_scenes` independent box-drop scenes.  Each has a
+    particle count log-uniform in [n_min, n_max], radii uniform in
+    [0.9, 1.1] mm, its own closed box tilted 30 degrees (12 k^2 triangles, k in
+    1..13, so 12 to 2,028), sized so its spheres start on a loose lattice in
+    the middle, and its own friction mu in [0.2, 0.7] and restitution e in
+    [0.3, 0.9].  Hertz-Mindlin, E = 5e6 Pa, nu = 0.3, dt = 1e-6 s."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for s in range(n_scenes):
+        n = int(round(math.exp(rng.uniform(math.log(n_min), math.log(n_max)))))
+        radii = rng.uniform(0.9e-3, 1.1e-3, n)
+        rmax = float(radii.max())
+        a = 2.0 * rmax * 1.05
+        per_axis = math.ceil(n ** (1.0 / 3.0)) + 1
+        half = (per_axis * a + 2 * rmax) / 0.9          # lattice region = middle 90 % of the half-size
+        k = int(rng.integers(1, 14))
+        tris = rotate_z(box_mesh_grid(half, k), 30.0)
+        lo = np.full(3, -0.45 * half)
+        hi = np.full(3, 0.45 * half)
+        x = lattice_packing(n, radii, lo, hi, rng, gap=0.05)
+        m = sphere_mass(2500.0, radii)
+        kk = np.full(n, stiffness_from_E(5e6, 1e-3))
+        mu = float(rng.uniform(0.2, 0.7))
+        e = float(rng.uniform(0.3, 0.9))
+        out.append(Scene(x=x, r=radii, m=m, k=kk, eta=eta_const(kk, e), mu=mu, dt=1e-6, tris=tris,
+                         inlet_lo=lo, inlet_hi=hi, E=5e6, nu=0.3, e=e, name=f"batch-{s}-{n}"))
+    return out
+
+
+def pack_scenes(scenes: list, gap=None):
+    """Independent scenes side by side in one domain, for one engine: their
+    bounding boxes (mesh and spheres) shelf-packed `gap` apart (default eight
+    maximum radii, well beyond the Verlet cutoff, so no two scenes ever list
+    each other), every scene translated by its offset.  Returns the packed
+    Scene, with per-particle friction and restitution, and the offsets (S, 3)
+    and particle ranges (S + 1,)."""
+    rmax = max(float(np.max(sc.r)) for sc in scenes)
+    gap = 8.0 * rmax if gap is None else gap
+    lo = [np.minimum(sc.tris.reshape(-1, 3).min(0), np.asarray(sc.x).min(0) - rmax) for sc in scenes]
+    hi = [np.maximum(sc.tris.reshape(-1, 3).max(0), np.asarray(sc.x).max(0) + rmax) for sc in scenes]
+    ext = [h - l + gap for l, h in zip(lo, hi)]
+    width = 1.3 * sum(float(np.prod(e)) for e in ext) ** (1.0 / 3.0)
+    order = sorted(range(len(scenes)), key=lambda s: -float(np.max(ext[s])))
+    offs = np.zeros((len(scenes), 3))
+    x0 = z0 = y0 = 0.0
+    row_d = layer_h = 0.0
+    for s in order:
+        e = ext[s]
+        if x0 + e[0] > width and x0 > 0:
+            x0, z0 = 0.0, z0 + row_d
+            row_d = 0.0
+        if z0 + e[2] > width and z0 > 0:
+            x0, z0, y0 = 0.0, 0.0, y0 + layer_h
+            row_d = layer_h = 0.0
+        offs[s] = np.array([x0, y0, z0]) - lo[s]
+        x0 += e[0]
+        row_d = max(row_d, e[2])
+        layer_h = max(layer_h, e[1])
+    cat = lambda f: np.concatenate([f(s, sc) for s, sc in enumerate(scenes)], 0)
+    x = cat(lambda s, sc: np.asarray(sc.x) + offs[s])
+    tris = cat(lambda s, sc: np.asarray(sc.tris) + offs[s])
+    zeros3 = lambda sc: np.zeros((sc.n, 3))
+    v = cat(lambda s, sc: np.asarray(sc.v) if sc.v is not None else zeros3(sc))
+    w = cat(lambda s, sc: np.asarray(sc.w) if sc.w is not None else zeros3(sc))
+    starts = np.concatenate([[0], np.cumsum([sc.n for sc in scenes])])
+    first = scenes[0]
+    packed = Scene(x=x, r=cat(lambda s, sc: sc.r), m=cat(lambda s, sc: sc.m), k=cat(lambda s, sc: sc.k),
+                   eta=cat(lambda s, sc: sc.eta), mu=first.mu, dt=first.dt, tris=tris,
+                   inlet_lo=x.min(0) - rmax, inlet_hi=x.max(0) + rmax, g=first.g, v=v, w=w,
+                   E=first.E, nu=first.nu, e=first.e, mu_roll=first.mu_roll,
+                   mu_p=cat(lambda s, sc: np.full(sc.n, sc.mu)), e_p=cat(lambda s, sc: np.full(sc.n, sc.e)),
+                   name=f"packed-{len(scenes)}-scenes")
+    return packed, offs, starts

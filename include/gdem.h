@@ -172,6 +172,14 @@ int gdem_import_particles(gdem_handle* h, const gdem_particles* p);
 int gdem_step(gdem_handle* h, int nsteps);
 int gdem_synchronize(gdem_handle* h);   /* wait; GDEM_ERR_DEVICE if the error word is set */
 
+/* Hertz-Mindlin friction coefficient and restitution per particle (pId
+ * order, n values each), in place of the engine-wide mu and restitution: for
+ * several independent scenes packed into one engine, each with its own
+ * material.  Both particles of a contact must carry the same values.  Call
+ * after gdem_import_particles; a later import clears them.  No counterpart in
+ * the reference (its material is global, ParticleSysShared::mu). */
+int gdem_set_particle_materials(gdem_handle* h, const double* mu, const double* restitution);
+
 /* Download in pId order (replaces copyFromDevice, ParticleSystem.cu:97).
  * Fields left NULL are skipped. */
 int gdem_export_particles(gdem_handle* h, gdem_particles* p);
