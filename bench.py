@@ -36,6 +36,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "particle-steps/s at 1M spheres, FP32-mixed vs FP64 plain on 1 GB300 (err≤1e-4·r_min)"
+TRAFFIC_POURED_BED_1M = 809_291_520.0   # bytes per step-kernel launch, ncu on the default workload
 UNIT = "particle-steps/s"
 
 
@@ -103,6 +104,20 @@ def algorithmic_bytes(st, n_active, s=8, s_h=8):
     s_write = 24 + 6 * s
     return (n_active * (s_read + s_write) + 4 * (2 * n_active + st["n_nei"] + st["n_wall"])
             + (st["n_contacts"] + st["n_wall_contacts"]) * (6 * s_h + 8))
+
+
+def aggregate_replicas(ms, n_active, steps, dist=None):
+    """Whole-job numbers of N replicas: the slowest rank's time, and the
+    particle-steps of all ranks over that time (each rank steps its own
+    copy of the workload)."""
+    import torch
+    work = torch.tensor([float(n_active) * steps], dtype=torch.float64)
+    t = torch.tensor([float(ms)], dtype=torch.float64)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.all_reduce(work, op=dist.ReduceOp.SUM)
+    ms = float(t.item())
+    return ms, float(work.item()) / (ms / 1e3)
 
 
 def dist_init():
@@ -183,12 +198,7 @@ def run_engine(args):
     out_dir = os.path.join(ROOT, "gpurun_out") if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp"
     clk = Clocks(os.path.join(out_dir, f"clocks_r{rank}.csv"))
     ms, st0, st1 = _time_steps(E, args.steps, args.warmup, stream, clk)
-    if dist:
-        t = torch.tensor([ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    n_act = 0.5 * (st0["n_active"] + st1["n_active"])
-    value = n_act * args.steps * ws / (ms / 1e3)
+    ms, value = aggregate_replicas(ms, 0.5 * (st0["n_active"] + st1["n_active"]), args.steps, dist)
     # dominant kernel: the step kernel alone, CUDA events on the engine stream
     _nvtx("profile")
     k_ms = E.profile_step(args.profile_iters)
@@ -198,6 +208,11 @@ def run_engine(args):
     bytes_launch = algorithmic_bytes(stk, stk["n_active"], s=4 if mixed else 8, s_h=8)
     peak, peak_kind = _peaks()
     achieved = bytes_launch / (k_ms / 1e3) / 1e9
+    traffic = args.traffic
+    if traffic is None and mixed and args.workload == "poured" and args.n == 1_000_000 and args.model == "hertz_mindlin":
+        # dram__bytes_read.sum + dram__bytes_write.sum of one launch on this
+        # workload (profiles/k_step_mixed_coop_poured_bed_1M.txt)
+        traffic = TRAFFIC_POURED_BED_1M
     reb = int(st1["rebuilds"] - st0["rebuilds"])
     E.close()
     extra = {}
@@ -249,7 +264,7 @@ def run_engine(args):
         # clear, cell ranges, Verlet (+ the FP32 position copy in FP64 mode), walls)
         "gpu_launches": args.steps * (1 + (0 if args.bvh_once else 16)) + reb * 19,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": args.traffic,
+                     "frac": achieved / peak, "traffic": traffic,
                      "peak_kind": f"{peak_kind} hbm_gbs",
                      "kernel": f"k_step<{'Mixed' if mixed else 'FP64'},{args.model}>", "kernel_ms": k_ms,
                      "algorithmic_bytes": bytes_launch,
@@ -370,6 +385,13 @@ def run_batched(args):
     scs = scenes.config4_batched(n_scenes=args.n_scenes)
     packed, offs, starts = scenes.pack_scenes(scs)
     kw = dict(model="hertz_mindlin", steps_per_graph=8)
+    tuned = None
+    if args.autotune:
+        from gpudem_gb300 import autotune
+        t0 = time.time()
+        tuned = autotune.autotune(packed, precision=args.precision, model="hertz_mindlin", steps=32, warmup=8)
+        kw.update(tuned.settings)
+        tune_s = time.time() - t0
     E = engine.Engine(packed, precision=args.precision, **kw)
     stream = torch.cuda.ExternalStream(E.stream())
     out_dir = os.path.join(ROOT, "gpurun_out") if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp"
@@ -401,6 +423,9 @@ def run_batched(args):
                                   f"{packed.tris.shape[0]} triangles in all (per scene "
                                   f"{min(sc.tris.shape[0] for sc in scs)}..{max(sc.tris.shape[0] for sc in scs)}), "
                                   f"hertz_mindlin, per-scene mu and e, {args.precision}",
+                      "autotuned": None if tuned is None else {k: (round(v, 7) if isinstance(v, float) else v)
+                                                               for k, v in tuned.settings.items()},
+                      "autotune_s": None if tuned is None else round(tune_s, 1),
                       "one_by_one_value": seq_value, "one_by_one_steps_per_scene": seq_steps,
                       "batched_over_one_by_one": value / seq_value, "rebuilds_in_timed_region": reb},
            "clocks": clk.summary(), "gpu_launches": args.steps + reb * 19}
@@ -430,6 +455,8 @@ def main():
     ap.add_argument("--workload", default="poured", choices=["poured", "lattice", "batched"])
     ap.add_argument("--n-scenes", type=int, default=256)
     ap.add_argument("--seq-steps", type=int, default=200)
+    ap.add_argument("--autotune", action="store_true",
+                    help="batched workload: tune kernel, occupancy, skin, cell size and graph length first")
     ap.add_argument("--bvh-once", action="store_true",
                     help="build the static mesh's LBVH once instead of in every step")
     ap.add_argument("--settle-steps", type=int, default=12000)

@@ -44,7 +44,7 @@ class Desc(C.Structure):
         ("cell_size", C.c_double), ("skin", C.c_double), ("refresh_thresh", C.c_double),
         ("youngs_modulus", C.c_double), ("poisson_ratio", C.c_double),
         ("restitution", C.c_double), ("rolling_friction", C.c_double),
-        ("bvh_every_step", C.c_int),
+        ("bvh_every_step", C.c_int), ("mixed_kernel", C.c_int), ("occupancy", C.c_int),
     ]
 
 

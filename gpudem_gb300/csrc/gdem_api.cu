@@ -149,6 +149,8 @@ struct Impl : EngineBase {
         v.hist_cap = d.hist_capacity;
         v.histw_cap = d.hist_wall_capacity;
         v.store_forces = d.store_forces ? 1 : 0;
+        v.kernel_variant = d.mixed_kernel >= 0 && d.mixed_kernel <= 3 ? d.mixed_kernel : 0;
+        v.occupancy = d.occupancy > 0 ? d.occupancy : 0;
         v.reorder = d.reorder == 0 ? 0 : 1;
         v.rs_blocks = rs_blocks_for(n);
         const size_t H = (size_t)n * v.hist_cap, HW = (size_t)n * v.histw_cap;

@@ -176,6 +176,8 @@ struct View {
     float boxf[6];                   // mixed mode: box rounded outwards to FP32
     float nb_delta;                  // bound on |d_fp32 - d| of the list prefilter (m)
     int per_particle_mat;            // Hertz-Mindlin: mu and damping from mat.x, mat.y of each particle
+    int kernel_variant;              // mixed step kernel: 0 default, 1 cooperative, 2 staged, 3 one-pass
+    int occupancy;                   // mixed step kernel: resident CTAs per SM to size for (0 default)
     // the scalars above rounded to FP32 once, for the mixed step
     float dtf, gxf, gyf, gzf, thresh_sqf;
     float muf, kn_cf, sn_cf, kt_cf, damp_cf, mu_rollf;

@@ -1087,11 +1087,8 @@ __global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<
 }
 
 namespace {
-// MINB: resident blocks per SM the register allocation of the one-pass
-// kernel is sized for (2, the default: no spills; 3: more warps in flight,
-// with spills).  GDEM_MIXED_MINB picks one.  GDEM_MIXED_KERNEL=staged picks
-// the warp-staged persistent kernel, =direct the one-pass kernel, instead of
-// the warp-cooperative one.
+// MINB: resident CTAs per SM a kernel's register allocation is sized for
+// (cooperative kernel 4, 5 or 6; one-pass kernel 2 or 3).
 template <int MODEL, int MINB>
 void* direct_kernel_minb(int wall_cap) {
     if (wall_cap <= 16) return (void*)k_step_mixed<MODEL, 16, MINB>;
@@ -1099,11 +1096,7 @@ void* direct_kernel_minb(int wall_cap) {
     return (void*)k_step_mixed<MODEL, 64, MINB>;
 }
 template <int MODEL>
-void* direct_kernel(int wall_cap) {
-    static const int minb = [] {
-        const char* e = getenv("GDEM_MIXED_MINB");
-        return e ? atoi(e) : 2;
-    }();
+void* direct_kernel(int wall_cap, int minb) {
     return minb == 3 ? direct_kernel_minb<MODEL, 3>(wall_cap) : direct_kernel_minb<MODEL, 2>(wall_cap);
 }
 template <int MODEL>
@@ -1132,20 +1125,20 @@ void* coop_kernel_minb(int wall_cap) {
     }
     return fn;
 }
-// resident CTAs per SM the cooperative kernel's registers are sized for
-// (GDEM_COOP_MINB: 4, 5 or 6; 5 by default)
 template <int MODEL>
-void* coop_kernel(int wall_cap) {
-    static const int minb = [] {
-        const char* e = getenv("GDEM_COOP_MINB");
-        const int m = e ? atoi(e) : 5;
-        return m == 4 || m == 6 ? m : 5;
-    }();
+void* coop_kernel(int wall_cap, int minb) {
     return minb == 4 ? coop_kernel_minb<MODEL, 4>(wall_cap)
                      : (minb == 6 ? coop_kernel_minb<MODEL, 6>(wall_cap) : coop_kernel_minb<MODEL, 5>(wall_cap));
 }
-// 0: warp-cooperative (default), 1: warp-staged, 2: direct
-int kernel_kind() {
+// Kernel and occupancy: the engine's settings, else the environment
+// (GDEM_MIXED_KERNEL=staged|direct, GDEM_COOP_MINB, GDEM_MIXED_MINB), else the
+// defaults (warp-cooperative, 5 CTAs per SM).
+int env_int(const char* name, int dflt) {
+    const char* e = getenv(name);
+    return e ? atoi(e) : dflt;
+}
+int kernel_kind(const View<Mixed>& v) {
+    if (v.kernel_variant > 0) return v.kernel_variant - 1;
     static const int k = [] {
         const char* e = getenv("GDEM_MIXED_KERNEL");
         if (e && strcmp(e, "direct") == 0) return 2;
@@ -1167,9 +1160,11 @@ int sm_count() {
 
 StepLaunch step_launch(const View<Mixed>& v) {
     const int ntiles = (v.n + kBlock - 1) / kBlock;
-    const int kind = kernel_kind();
+    const int kind = kernel_kind(v);
     if (kind == 0) {
-        void* fn = v.mat.model == 1 ? coop_kernel<1>(v.wall_cap) : coop_kernel<0>(v.wall_cap);
+        static const int env_minb = env_int("GDEM_COOP_MINB", 5);
+        const int minb = v.occupancy > 0 ? v.occupancy : env_minb;
+        void* fn = v.mat.model == 1 ? coop_kernel<1>(v.wall_cap, minb) : coop_kernel<0>(v.wall_cap, minb);
         const size_t smem = kCoopSmem;
         int per_sm = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kCoopWarps * 32, smem);
@@ -1186,7 +1181,9 @@ StepLaunch step_launch(const View<Mixed>& v) {
         const int grid = need < 2 * sm_count() ? need : 2 * sm_count();
         return StepLaunch{fn, dim3(grid), dim3(kBlock), (size_t)2 * kWarps * kWStageBytes};
     }
-    void* fn = v.mat.model == 1 ? direct_kernel<1>(v.wall_cap) : direct_kernel<0>(v.wall_cap);
+    static const int env_minb = env_int("GDEM_MIXED_MINB", 2);
+    const int minb = v.occupancy > 0 ? v.occupancy : env_minb;
+    void* fn = v.mat.model == 1 ? direct_kernel<1>(v.wall_cap, minb) : direct_kernel<0>(v.wall_cap, minb);
     return StepLaunch{fn, dim3(ntiles), dim3(kBlock), 0};
 }
 

@@ -48,7 +48,7 @@ class Engine:
     def __init__(self, scene: Scene, precision="fp64", model="linear", reorder=True,
                  store_forces=False, nei_capacity=64, wall_capacity=32, hist_capacity=32,
                  hist_wall_capacity=16, steps_per_graph=8, cell_size=-1.0, skin=None,
-                 refresh=None, box=None, bvh_every_step=False):
+                 refresh=None, box=None, bvh_every_step=False, mixed_kernel=0, occupancy=0):
         self.L = _lib.load()
         self.scene = scene
         self.n = scene.n
@@ -80,6 +80,8 @@ class Engine:
         d.restitution = scene.e
         d.rolling_friction = scene.mu_roll
         d.bvh_every_step = 1 if bvh_every_step else 0
+        d.mixed_kernel = int(mixed_kernel)
+        d.occupancy = int(occupancy)
         self.desc = d
         h = C.c_void_p()
         _lib.check(self.L.gdem_create(C.byref(d), C.byref(h)), None, "gdem_create")

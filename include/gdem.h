@@ -80,6 +80,10 @@ typedef struct gdem_desc {
     double rolling_friction;
     int bvh_every_step;     /* 1: rebuild the mesh LBVH (keys, sort, nodes, boxes) in every step, as a
                                moving mesh needs; 0 (default): build it once when the mesh is set */
+    /* mixed-precision step kernel (results are the same for every choice):
+     * 0 default (warp-cooperative), 1 warp-cooperative, 2 warp-staged, 3 one thread per particle */
+    int mixed_kernel;
+    int occupancy;          /* resident CTAs per SM its registers are sized for; 0: default (4..6 / 2..3) */
 } gdem_desc;
 
 /* Particle arrays in the reference layout (memberList/ParticleSystemMember_common.def).
