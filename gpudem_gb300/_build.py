@@ -55,7 +55,7 @@ def _stale(target, sources):
     if not os.path.exists(target):
         return True
     t = os.path.getmtime(target)
-    return any(os.path.getmtime(s) > t for s in sources)
+    return any(os.path.exists(s) and os.path.getmtime(s) > t for s in sources)
 
 
 def build_engine(verbose=False, ptxas_info=False) -> str:
@@ -88,7 +88,7 @@ def build_oracle() -> str:
     """Compile the CPU restatement (test infrastructure) with the host
     compiler, no FMA contraction, OpenMP for the timed CPU baseline."""
     os.makedirs(OUT, exist_ok=True)
-    if _stale(ORACLE_LIB, [ORACLE_SRC, __file__, ORACLE_SRC.replace(".cpp", ".h")]):
+    if _stale(ORACLE_LIB, [ORACLE_SRC, __file__]):
         _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
               "-fno-fast-math", ORACLE_SRC, "-o", ORACLE_LIB])
     return ORACLE_LIB

@@ -8,8 +8,8 @@ of each candidate on the GPU.  The skin, cell size and graph length leave the
 trajectory unchanged: the lists only decide which pairs are tested, the
 contact set is the same while they are valid, and forces are summed in
 partner-pId order whatever the storage order.  The kernel variants compute
-the same contact law and differ only in FP32 rounding.  So the choice is
-about speed alone.
+the same contact law with the same FP32 operations (their trajectories are
+bit-identical on the GPU).  So the choice is about speed alone.
 
 The search is greedy, one parameter at a time in the order above, each stage
 keeping the best setting of the stages before it.

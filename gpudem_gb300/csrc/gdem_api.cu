@@ -9,6 +9,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <cmath>
 #include <memory>
 #include <string>
 #include <unordered_map>
@@ -58,6 +59,7 @@ struct MeshData {
     char* seg = nullptr;                       // segment tree of leaf boxes
     unsigned* done = nullptr;                  // last-CTA counter of the tree build
     double gmin[3] = {0., 0., 0.}, ginv[3] = {0., 0., 0.};
+    double max_diag = 0.;                      // largest triangle bounding-box diagonal
     std::vector<double> aabb_h;
 };
 
@@ -263,11 +265,19 @@ struct Impl : EngineBase {
         if (T::mixed) {
             cudaFree(trif);
             trif = nullptr;
-            if (M.ntri > 0 && cudaMalloc((void**)&trif, sizeof(TriRecF) * M.ntri) == cudaSuccess) {
-                launch_trif(M.rec, trif, M.ntri, st);
+            TriLoF* lo = nullptr;
+            const size_t hb = sizeof(TriRecF) * (size_t)M.ntri;
+            if (M.ntri > 0 && cudaMalloc((void**)&trif, hb + sizeof(TriLoF) * (size_t)M.ntri) == cudaSuccess) {
+                lo = reinterpret_cast<TriLoF*>(reinterpret_cast<char*>(trif) + hb);
+                launch_trif(M.rec, trif, lo, M.ntri, st);
                 cudaStreamSynchronize(st);
             }
             v.trif = trif;
+            v.trilo = lo;
+            // the FP32 closest-feature distance is within a few ulp of the
+            // corner-relative vector (at most the triangle's diagonal plus the
+            // radius); 2^-16 of the diagonal bounds that with a wide margin
+            v.wall_delta = (float)std::ldexp(M.max_diag, -16);
         }
     }
 
@@ -1000,6 +1010,12 @@ static int upload_mesh(gdem_handle* h, const std::vector<double>& vx, const std:
             if (M.aabb_h[6 * t + k] < g[k]) g[k] = M.aabb_h[6 * t + k];
         for (int k = 0; k < 3; k++)
             if (M.aabb_h[6 * t + 3 + k] > g[3 + k]) g[3 + k] = M.aabb_h[6 * t + 3 + k];
+        double d2 = 0.;
+        for (int k = 0; k < 3; k++) {
+            const double e = M.aabb_h[6 * t + 3 + k] - M.aabb_h[6 * t + k];
+            d2 += e * e;
+        }
+        if (d2 > M.max_diag * M.max_diag) M.max_diag = std::sqrt(d2);
     }
     const int SCALE = (1 << 10) - 1;
     double inv[3];

@@ -2,7 +2,8 @@
 //
 // Per-particle data that neighbours gather lives in 16/32-byte records, so a
 // neighbour costs three vector loads:
-//   pos[i] = {x, y, z, r}           double4_32a (positions stay FP64 in every mode)
+//   pos[i] = {x, y, z, r}           double4_32a (FP64 mode); mixed mode keeps the
+//                                   float pairs posh/posl instead (SBank)
 //   vel[i] = {vx, vy, vz, 1/m}      V4 (double4_32a in FP64 mode, float4 in mixed mode)
 //   rot[i] = {wx, wy, wz, status}   V4; status 1 active, 0 inactive, 2 leaving the
 //                                   box this step (still in this step's rebuild)
@@ -69,6 +70,15 @@ struct __align__(16) TriRecF {
     int pad;
 };
 static_assert(sizeof(TriRecF) == 128, "TriRecF must be 128 bytes");
+
+// Low parts of a mixed-mode triangle: with TriRecF's n, e01 and e02 they give
+// the unit normal and the edges from the first corner as float pairs, for the
+// overlap of a wall contact (48 bytes, read only for contacts).
+struct __align__(16) TriLoF {
+    float nl[3], e01l[3], e02l[3];
+    float pad[3];
+};
+static_assert(sizeof(TriLoF) == 48, "TriLoF must be 48 bytes");
 
 struct Ctl {
     int s;                    // state bank holding the current state
@@ -163,6 +173,8 @@ struct View {
     // mesh
     const TriRec* tri;
     const TriRecF* trif;             // mixed mode
+    const TriLoF* trilo;             // mixed mode
+    float wall_delta;                // mixed mode: bound on the FP32 error of a wall distance (m)
     const BNode* bvh;
     int ntri;
     int bvh_root;
@@ -379,7 +391,7 @@ void radix_sort_pairs(uint32_t* keys0, int* vals0, uint32_t* keys1, int* vals1, 
 int rs_blocks_for(int n);
 void launch_dist_triangle(const TriRec* tri, const double* pos, const double* r, const int* t, int m,
                           double* out4, int* hit, cudaStream_t st);
-void launch_trif(const TriRec* tri, TriRecF* out, int ntri, cudaStream_t st);
+void launch_trif(const TriRec* tri, TriRecF* out, TriLoF* lo, int ntri, cudaStream_t st);
 
 // float pair split of an FP64 value: x == hi + lo to within 2^-48 |x|
 __device__ __forceinline__ void split2(double x, float& hi, float& lo) {

@@ -878,29 +878,33 @@ size_t bvh_scratch_bytes(int ntri) {
     return sizeof(SegBox) * (size_t)seg_offset(ntri, levels);
 }
 
-// FP32 copy of the triangles for the mixed-precision step kernel.
-__global__ void k_trif(const TriRec* tri, TriRecF* out, int ntri) {
+// FP32 copy of the triangles for the mixed-precision step kernel, and the
+// low parts of its normal and corner-0 edges.
+__global__ void k_trif(const TriRec* tri, TriRecF* out, TriLoF* lo, int ntri) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ntri) return;
     const TriRec& T = tri[t];
     TriRecF F;
+    TriLoF L;
     for (int k = 0; k < 3; k++) {
         split2(T.v0[k], F.v0h[k], F.v0l[k]);
-        F.n[k] = (float)T.n[k];
-        F.e01[k] = (float)T.e01[k];
-        F.e02[k] = (float)T.e02[k];
+        split2(T.n[k], F.n[k], L.nl[k]);
+        split2(T.e01[k], F.e01[k], L.e01l[k]);
+        split2(T.e02[k], F.e02[k], L.e02l[k]);
         F.e12[k] = (float)T.e12[k];
+        L.pad[k] = 0.f;
     }
     F.d00 = (float)T.d00; F.d01 = (float)T.d01; F.d11 = (float)T.d11; F.denom = (float)T.denom;
     F.d00inv = (float)T.d00inv; F.d11inv = (float)T.d11inv; F.d22inv = (float)T.d22inv;
     F.i0 = T.i0; F.i1 = T.i1; F.i2 = T.i2; F.e0 = T.e0; F.e1 = T.e1; F.e2 = T.e2;
     F.pad = 0;
     out[t] = F;
+    lo[t] = L;
 }
 
-void launch_trif(const TriRec* tri, TriRecF* out, int ntri, cudaStream_t st) {
+void launch_trif(const TriRec* tri, TriRecF* out, TriLoF* lo, int ntri, cudaStream_t st) {
     if (ntri <= 0) return;
-    k_trif<<<grid_for(ntri), kBlock, 0, st>>>(tri, out, ntri);
+    k_trif<<<grid_for(ntri), kBlock, 0, st>>>(tri, out, lo, ntri);
 }
 
 // ===================================================================== probes

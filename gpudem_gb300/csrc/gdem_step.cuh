@@ -430,7 +430,7 @@ __global__ void __launch_bounds__(kBlock) k_step(View<T> v, cudaGraphConditional
                 const double4_32a rf = v.ref[i];
                 const double ex = nxp - rf.x, ey = nyp - rf.y, ez = nzp - rf.z;
                 const double d2 = ex * ex + ey * ey + ez * ez;
-                refresh = d2 > v.thresh_sq;
+                if (d2 > v.thresh_sq) refresh = true;
             }
             // ---------------- out of bounds (checkOoB, cpu_dem.cu:1575).  The
             // reference CPU loop deactivates after the list rebuild of this

@@ -32,6 +32,8 @@ namespace {
 struct FeatureF {
     float nx, ny, nz, dist;
     int hit;
+    int kind;  // 0 face; 1, 2, 3 corner 0, 1, 2; 4 edge 1-2, 5 edge 0-2, 6 edge 0-1
+    float t;   // edge parameter from the edge's first corner
 };
 
 // Closest feature of triangle T to the sphere centre (ph + pl) within radius^2
@@ -42,6 +44,8 @@ __device__ __forceinline__ FeatureF closest_feature_f(float3 ph, float3 pl, floa
     res.nx = res.ny = res.nz = 0.f;
     res.dist = 1.e10f;
     res.hit = -2;
+    res.kind = 0;
+    res.t = 0.f;
     const float ax = (ph.x - T.v0h[0]) + (pl.x - T.v0l[0]);
     const float ay = (ph.y - T.v0h[1]) + (pl.y - T.v0l[1]);
     const float az = (ph.z - T.v0h[2]) + (pl.z - T.v0l[2]);
@@ -62,33 +66,42 @@ __device__ __forceinline__ FeatureF closest_feature_f(float3 ph, float3 pl, floa
         return res;
     }
     float rx, ry, rz;  // centre minus the closest point
-    int hit;
+    int hit, kind;
+    float t = 0.f;
     if (v <= 0.f && w <= 0.f) {
         rx = ax; ry = ay; rz = az;
         hit = T.i0;
+        kind = 1;
     } else if (u <= 0.f && w <= 0.f) {
         rx = ax - T.e01[0]; ry = ay - T.e01[1]; rz = az - T.e01[2];
         hit = T.i1;
+        kind = 2;
     } else if (u <= 0.f && v <= 0.f) {
         rx = ax - T.e02[0]; ry = ay - T.e02[1]; rz = az - T.e02[2];
         hit = T.i2;
+        kind = 3;
     } else if (u <= 0.f) {
         const float bx = ax - T.e01[0], by = ay - T.e01[1], bz = az - T.e01[2];
-        float t = (bx * T.e12[0] + by * T.e12[1] + bz * T.e12[2]) * T.d22inv;
+        t = (bx * T.e12[0] + by * T.e12[1] + bz * T.e12[2]) * T.d22inv;
         t = fmaxf(0.f, fminf(1.f, t));
         rx = bx - t * T.e12[0]; ry = by - t * T.e12[1]; rz = bz - t * T.e12[2];
         hit = T.e1;
+        kind = 4;
     } else if (v <= 0.f) {
-        float t = d21 * T.d11inv;
+        t = d21 * T.d11inv;
         t = fmaxf(0.f, fminf(1.f, t));
         rx = ax - t * T.e02[0]; ry = ay - t * T.e02[1]; rz = az - t * T.e02[2];
         hit = T.e2;
+        kind = 5;
     } else {
-        float t = d20 * T.d00inv;
+        t = d20 * T.d00inv;
         t = fmaxf(0.f, fminf(1.f, t));
         rx = ax - t * T.e01[0]; ry = ay - t * T.e01[1]; rz = az - t * T.e01[2];
         hit = T.e0;
+        kind = 6;
     }
+    res.kind = kind;
+    res.t = t;
     const float dsq = rx * rx + ry * ry + rz * rz;
     if (dsq < rsq) {
         const float inv = rsqrtf(dsq);
@@ -177,6 +190,103 @@ __device__ __forceinline__ int contact_hint(float4 hi, float4 hj, float delta) {
 // high parts leave undecided; kept out of line so the scan loop stays small.
 __device__ __noinline__ bool exact_contact(float4 hi, float4 li, float4 hj, float4 lj) {
     return pair_geometry(hi, li, hj, lj).num > 0.f;
+}
+
+// a + b as an unevaluated pair (s, e), exactly
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) { two_diff(a, -b, s, e); }
+
+// a * b as an unevaluated pair (p, e), exactly (FMA)
+__device__ __forceinline__ void two_prod(float a, float b, float& p, float& e) {
+    p = __fmul_rn(a, b);
+    e = __fmaf_rn(a, b, -p);
+}
+
+// Overlap (r_h + r_l) - dist of the sphere centred at ph + pl with the feature
+// of triangle T that closest_feature_f picked (kind, and t on an edge), to
+// about FP64 accuracy.  The centre minus the closest point is formed as float
+// pairs from corner 0 and the two edges from it (high parts in T, low parts in
+// L); on a face its normal component comes from error-free products with the
+// unit normal as a pair, on an edge or corner its squared length from
+// error-free squares, and the overlap is (r^2 - |u|^2) / (r + |u|) without
+// cancellation.  An edge's distance is stationary in t, so the FP32 t costs
+// nothing to first order.  Only contacts come here.
+__device__ __forceinline__ float wall_overlap(float3 ph, float3 pl, float rh, float rl, const TriRecF& T,
+                                           const TriLoF& L, int kind, float t) {
+    const float P[3] = {ph.x, ph.y, ph.z}, Pl[3] = {pl.x, pl.y, pl.z};
+    float qh[3], ql[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        float e;
+        two_diff(P[k], T.v0h[k], qh[k], e);
+        ql[k] = __fadd_rn(e, __fsub_rn(Pl[k], T.v0l[k]));
+    }
+    if (kind == 0) {
+        float s, lo, p, e;
+        two_prod(T.n[0], qh[0], s, lo);
+#pragma unroll
+        for (int k = 1; k < 3; k++) {
+            float pe;
+            two_prod(T.n[k], qh[k], p, pe);
+            two_sum(s, p, s, e);
+            lo = __fadd_rn(lo, __fadd_rn(e, pe));
+        }
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+            lo = __fadd_rn(lo, __fadd_rn(__fmul_rn(T.n[k], ql[k]), __fmul_rn(L.nl[k], qh[k])));
+        if (s < 0.f) {
+            s = -s;
+            lo = -lo;
+        }
+        float dh, de;
+        two_diff(rh, s, dh, de);
+        return __fadd_rn(dh, __fadd_rn(de, __fsub_rn(rl, lo)));
+    }
+    float uh[3], ul[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        float ah = qh[k], al = ql[k], e;
+        if (kind == 2 || kind == 4) {  // from corner 1
+            two_diff(ah, T.e01[k], ah, e);
+            al = __fadd_rn(al, __fsub_rn(e, L.e01l[k]));
+        } else if (kind == 3) {        // corner 2
+            two_diff(ah, T.e02[k], ah, e);
+            al = __fadd_rn(al, __fsub_rn(e, L.e02l[k]));
+        }
+        if (kind >= 4) {
+            float eh, el;
+            if (kind == 4) {
+                two_diff(T.e02[k], T.e01[k], eh, e);
+                el = __fadd_rn(e, __fsub_rn(L.e02l[k], L.e01l[k]));
+            } else if (kind == 5) {
+                eh = T.e02[k];
+                el = L.e02l[k];
+            } else {
+                eh = T.e01[k];
+                el = L.e01l[k];
+            }
+            float pt, et;
+            two_prod(t, eh, pt, et);
+            two_diff(ah, pt, ah, e);
+            al = __fadd_rn(al, __fsub_rn(__fsub_rn(e, et), __fmul_rn(t, el)));
+        }
+        uh[k] = ah;
+        ul[k] = al;
+    }
+    float D, lo, p, pe, e;
+    two_prod(uh[0], uh[0], D, lo);
+#pragma unroll
+    for (int k = 1; k < 3; k++) {
+        two_prod(uh[k], uh[k], p, pe);
+        two_sum(D, p, D, e);
+        lo = __fadd_rn(lo, __fadd_rn(e, pe));
+    }
+    const float cross = __fadd_rn(__fadd_rn(__fmul_rn(uh[0], ul[0]), __fmul_rn(uh[1], ul[1])), __fmul_rn(uh[2], ul[2]));
+    lo = __fadd_rn(lo, __fmul_rn(2.f, cross));
+    float R2, R2e, nh, ne;
+    two_prod(rh, rh, R2, R2e);
+    two_diff(R2, D, nh, ne);
+    const float num = __fadd_rn(nh, __fadd_rn(ne, __fsub_rn(__fadd_rn(R2e, __fmul_rn(2.f, __fmul_rn(rh, rl))), lo)));
+    return num / (rh + sqrtf(D));
 }
 
 }  // namespace
@@ -327,7 +437,9 @@ __device__ __forceinline__ void wall_forces(const View<Mixed>& v, const PBank<Mi
     int vore[WCAP];
     int nvore = 0;
     const float3 ph = make_float3(hi.x, hi.y, hi.z), pl = make_float3(li.x, li.y, li.z);
-    const R rsq = ri * ri;
+    // candidates within the FP32 error bound of touching go to the exact overlap
+    const R rm = ri + v.wall_delta;
+    const R rmsq = rm * rm;
     for (int k0 = 0; k0 < nw; k0 += 4) {
         // four candidates at a time: their indices, then the first 48 bytes
         // of their records (corner pair and normal), all in flight together,
@@ -346,14 +458,16 @@ __device__ __forceinline__ void wall_forces(const View<Mixed>& v, const PBank<Mi
             const float ay = (ph.y - a.y) + (pl.y - b.x);
             const float az = (ph.z - a.z) + (pl.z - b.y);
             const float dist = b.z * ax + b.w * ay + c.x * az;
-            if (!(dist * dist > rsq)) near |= 1u << q;
+            if (!(dist * dist > rmsq)) near |= 1u << q;
         }
         while (near) {
             const int q = __ffs(near) - 1;
             near &= near - 1u;
             const int t = __ldg(&neiw[(size_t)(k0 + q) * n + i]);
-            const FeatureF f = closest_feature_f(ph, pl, rsq, v.trif[t]);
-            if (!(f.dist < ri)) continue;
+            const FeatureF f = closest_feature_f(ph, pl, rmsq, v.trif[t]);
+            if (!(f.dist < rm)) continue;
+            const R delmag = wall_overlap(ph, pl, ri, li.w, v.trif[t], v.trilo[t], f.kind, f.t);
+            if (!(delmag > 0.f)) continue;
         if (f.hit != -1) {
             bool dup = false;
             for (int q = 0; q < nvore; q++)
@@ -364,7 +478,6 @@ __device__ __forceinline__ void wall_forces(const View<Mixed>& v, const PBank<Mi
             if (dup) continue;
             if (nvore < WCAP) vore[nvore++] = f.hit;
         }
-        const R delmag = ri - f.dist;
         const R nx = f.nx, ny = f.ny, nz = f.nz;
         const R vdn = vi.x * nx + vi.y * ny + vi.z * nz;
         const R vnx = vdn * nx, vny = vdn * ny, vnz = vdn * nz;
@@ -489,10 +602,11 @@ __device__ __forceinline__ void integrate_one(const View<Mixed>& v, const SBank<
     B.rotl[i] = wl;
     // refresh test against the position of the last rebuild, on the high
     // parts: it only decides when the lists are rebuilt, and the threshold
-    // leaves a margin of skin/2 to the list cutoff
+    // leaves a margin of skin/2 to the list cutoff.  The flag is sticky: the
+    // persistent kernels integrate many particles per thread.
     {
         const R ex = nh.x - o.rh.x, ey = nh.y - o.rh.y, ez = nh.z - o.rh.z;
-        refresh = ex * ex + ey * ey + ez * ez > v.thresh_sqf;
+        if (ex * ex + ey * ey + ez * ez > v.thresh_sqf) refresh = true;
     }
     // out of bounds (the box rounded outwards to FP32)
     R status = 1.f;

@@ -538,3 +538,72 @@ def pack_scenes(scenes: list, gap=None):
                    mu_p=cat(lambda s, sc: np.full(sc.n, sc.mu)), e_p=cat(lambda s, sc: np.full(sc.n, sc.e)),
                    name=f"packed-{len(scenes)}-scenes")
     return packed, offs, starts
+
+
+# --------------------------------------------------------------------------- physics checks
+# Small scenes for the reference's physics-level comparisons: the LIGGGHTS
+# two-sphere collision (liggghtsCases/testCases/in.collision) and the analytic
+# scripts python/compareDrop.py, compareRoll.py and compareCollision.py.
+
+def hooke_stiffness(Y: float, nu: float, r1: float, r2: float, m1: float, m2: float, v_char: float) -> float:
+    """Normal stiffness of LIGGGHTS' `hooke` pair model (its documented
+    formula): kn = 16/15 sqrt(R*) Y* (15 m* V^2 / (16 sqrt(R*) Y*))^(1/5) with
+    Y* = 1/((1-nu^2)/Y + (1-nu^2)/Y), R* = r1 r2/(r1+r2), m* = m1 m2/(m1+m2) and
+    V the characteristic velocity.  LIGGGHTS uses the same value tangentially."""
+    ystar = 1.0 / (2.0 * (1.0 - nu * nu) / Y)
+    rstar = r1 * r2 / (r1 + r2)
+    mstar = m1 * m2 / (m1 + m2)
+    sq = math.sqrt(rstar)
+    return 16.0 / 15.0 * sq * ystar * (15.0 * mstar * v_char * v_char / (16.0 * sq * ystar)) ** 0.2
+
+
+def hooke_eta_const(kn: float, e: float) -> float:
+    """etaconst for which the linear law's damping etaconst * sqrt(m*) equals
+    LIGGGHTS' hooke gamma_n = sqrt(4 m* kn / (1 + (pi / ln e)^2)), i.e. the
+    reference's formula (ParticleSystem.cu:301) with pi in full."""
+    le = math.log(e)
+    return -2.0 * le * math.sqrt(kn / (math.pi * math.pi + le * le))
+
+
+def two_sphere_scene(x, v, r, m, k, eta, mu: float, dt: float, half: float = 1.0) -> Scene:
+    """Two spheres without walls or gravity in the cube [-half, half]^3, with
+    the linear law's per-sphere k and etaconst."""
+    n = len(r)
+    return Scene(x=np.asarray(x, np.float64).reshape(n, 3), r=np.asarray(r, np.float64),
+                 m=np.asarray(m, np.float64), k=np.asarray(k, np.float64), eta=np.asarray(eta, np.float64),
+                 mu=mu, dt=dt, tris=np.zeros((0, 3, 3)), inlet_lo=np.full(3, -half),
+                 inlet_hi=np.full(3, half), g=np.zeros(3), v=np.asarray(v, np.float64).reshape(n, 3),
+                 w=np.zeros((n, 3)), name="two-spheres")
+
+
+def bouncing_sphere_scene(y0=0.5, floor=-1.0, r=0.01, rho=1000.0, k=1e5, e=0.3, mu=0.5, dt=5e-6) -> Scene:
+    """python/compareDrop.py's case: one sphere released at rest at height y0
+    above a horizontal floor (two triangles at y = floor), gravity -9.81 y."""
+    m = sphere_mass(rho, np.full(1, r))
+    kk = np.full(1, k)
+    a, b = 0.1, floor
+    tris = np.asarray(_quad(np.array([-a, b, -a]), np.array([-a, b, a]), np.array([a, b, a]),
+                            np.array([a, b, -a])), np.float64)
+    return Scene(x=np.array([[0.0, y0, 0.0]]), r=np.full(1, r), m=m, k=kk, eta=eta_const(kk, e), mu=mu, dt=dt,
+                 tris=tris, inlet_lo=np.array([-a, floor, -a]), inlet_hi=np.array([a, y0 + 2 * r, a]),
+                 v=np.zeros((1, 3)), w=np.zeros((1, 3)), e=e, name="bouncing-sphere")
+
+
+def incline_scene(theta_deg=60.0, mu=0.2, r=0.01, rho=1000.0, k=1e5, e=0.3, dt=1e-5, length=0.6) -> Scene:
+    """python/compareRoll.py's case: one sphere at rest on a plane inclined by
+    theta, descending along d = (cos theta, -sin theta, 0), touching at the
+    static overlap m g cos(theta) / k.  It slides with a = g (sin - mu cos)
+    when mu < 2/7 tan(theta) and rolls with a = 5/7 g sin otherwise."""
+    th = math.radians(theta_deg)
+    d = np.array([math.cos(th), -math.sin(th), 0.0])
+    nrm = np.array([math.sin(th), math.cos(th), 0.0])
+    z = np.array([0.0, 0.0, 1.0])
+    w = 0.05
+    tris = np.asarray(_quad(-0.05 * d - w * z, -0.05 * d + w * z, length * d + w * z, length * d - w * z), np.float64)
+    m = sphere_mass(rho, np.full(1, r))
+    kk = np.full(1, k)
+    x0 = (r - float(m[0]) * 9.81 * math.cos(th) / k) * nrm
+    v = tris.reshape(-1, 3)
+    return Scene(x=x0[None, :], r=np.full(1, r), m=m, k=kk, eta=eta_const(kk, e), mu=mu, dt=dt, tris=tris,
+                 inlet_lo=v.min(0) - 2 * r, inlet_hi=v.max(0) + 2 * r, v=np.zeros((1, 3)), w=np.zeros((1, 3)),
+                 e=e, name="incline")

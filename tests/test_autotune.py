@@ -39,7 +39,7 @@ def test_candidates_keep_the_cell_at_least_the_list_cutoff():
 @pytest.mark.gpu
 def test_tuned_engine_steps_the_same_trajectory():
     from gpudem_gb300 import autotune, engine, scenes
-    sc = scenes.config2_tilted_box(n=20_000)
+    sc = scenes.config2_tilted_box(n=5_000)
     t = autotune.autotune(sc, precision="mixed", model="hertz_mindlin", steps=16, warmup=4)
     assert t.ms_per_step > 0 and len(t.trials) == len(autotune.KERNELS) + len(autotune.SKIN_FACTORS) + len(
         autotune.GRAPH_STEPS)

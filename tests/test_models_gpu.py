@@ -103,6 +103,35 @@ def test_mixed_history_keys_follow_reorders():
     assert int(ha["numCont"].sum()) > 300
 
 
+def test_mixed_kernels_rebuild_with_fp64_while_pouring():
+    """300,000 spheres poured into the chute at dt = 2e-5 s, so the lists are
+    rebuilt every few steps.  Every mixed step kernel rebuilds at the steps
+    FP64 does: the persistent kernels integrate many particles per thread, and
+    every particle's refresh vote counts.  The three kernels step
+    bit-identical trajectories, and a repeat gives the same bits."""
+    from dataclasses import replace
+    from gpudem_gb300 import engine, scenes
+    sc = replace(scenes.config3_chute_pour(n=300_000), dt=2e-5, e=0.1)
+    kw = dict(model="hertz_mindlin", hist_capacity=32, hist_wall_capacity=16)
+
+    def run(precision, **k):
+        E = engine.Engine(sc, precision=precision, **kw, **k)
+        E.step(600)
+        x = E.export_positions()
+        st = E.stats()
+        E.close()
+        assert st["error_word"] == 0
+        return x, st["rebuilds"]
+
+    _, rf = run("fp64")
+    runs = [run("mixed", mixed_kernel=k) for k in (1, 2, 3, 1)]
+    print(f"pour, rebuilds in 600 steps: fp64 {rf}, mixed kernels {[r for _, r in runs]}")
+    assert rf >= 10
+    for x, rb in runs:
+        assert abs(rb - rf) <= 1
+        assert np.array_equal(x, runs[0][0])
+
+
 def test_mixed_error_on_the_poured_bed():
     """The benchmark workload: 1M lognormal spheres poured into the helical
     chute and settled (about 4.6 contacts per sphere), Hertz-Mindlin, the
