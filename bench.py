@@ -38,6 +38,7 @@ sys.path.insert(0, ROOT)
 METRIC = "particle-steps/s at 1M spheres, FP32-mixed vs FP64 plain on 1 GB300 (err≤1e-4·r_min)"
 TRAFFIC_POURED_BED_1M = 809_291_520.0   # bytes per step-kernel launch, ncu on the default workload
 UNIT = "particle-steps/s"
+METRIC_CHANNEL = "particle-steps/s at 10M spheres in a channel periodic in x, FP32-mixed on 1 GB300"
 
 
 def _peaks():
@@ -169,14 +170,34 @@ def _time_steps(E, steps, warmup, stream, clk=None, tag="timed"):
 
 
 def workload(args):
-    """The benchmark scene: the poured chute bed (default) or the loose
-    lattice over the chute with random velocities (`--workload lattice`)."""
+    """The benchmark scene: the poured chute bed (default), the loose lattice
+    over the chute with random velocities (`--workload lattice`), or the
+    channel periodic in x over a corrugated floor (`--workload channel`)."""
     from gpudem_gb300 import scenes
     if args.workload == "lattice":
         return scenes.config3_helical_chute(n=args.n, n_tri=args.ntri, v_sigma=args.v_sigma), 0.0
+    if args.workload == "channel":
+        return scenes.config5_periodic_channel(n=args.n, n_tri=args.ntri, v_sigma=args.v_sigma), 0.0
     t0 = time.time()
     sc = scenes.settle_scene(scenes.config3_chute_pour(n=args.n, n_tri=args.ntri), steps=args.settle_steps)
     return sc, time.time() - t0
+
+
+def describe(args, sc):
+    """(data, workload) strings of the bench line."""
+    if args.workload == "channel":
+        return ("synthetic (seeded bidisperse spheres on a lattice in a generated channel periodic in x)",
+                f"periodic channel 1 m (x, periodic) x 0.5 m, {sc.n} spheres r = 1.0 / 1.5 mm at 70 / 30, "
+                f"corrugated floor (amplitude 3 mm) + side walls, {sc.tris.shape[0]} triangles, dt=1e-6 s, "
+                f"{args.model} with rolling friction 0.05, {args.precision}, loose lattice, v_sigma "
+                f"{args.v_sigma} m/s")
+    chute = (f"helical chute, {sc.n} lognormal spheres (median 1 mm, sigma_log 0.15), "
+             f"{sc.tris.shape[0]} triangles, dt=1e-6 s, {args.model}, {args.precision}, ")
+    if args.workload == "poured":
+        return ("synthetic (seeded lognormal spheres poured into a generated helical chute, settled on the GPU "
+                "before timing)", chute + f"poured bed (settled {args.settle_steps} steps at dt=2e-5 s, e=0.1)")
+    return ("synthetic (seeded lognormal spheres on a lattice over a generated helical chute)",
+            chute + f"loose lattice, v_sigma {args.v_sigma} m/s")
 
 
 def run_engine(args):
@@ -237,18 +258,13 @@ def run_engine(args):
     # end to end through the C ABI with host buffers
     e2e = run_e2e(args, sc, kw) if not args.no_e2e else None
     out = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "metric": METRIC if args.workload != "channel" else METRIC_CHANNEL, "value": value, "unit": UNIT,
+        "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
         "dtype": "f32" if mixed else "f64",
-        "data": ("synthetic (seeded lognormal spheres poured into a generated helical chute, settled on the GPU "
-                 "before timing)" if args.workload == "poured" else
-                 "synthetic (seeded lognormal spheres on a lattice over a generated helical chute)"),
-        "config": {"workload": (f"helical chute, {args.n} lognormal spheres (median 1 mm, sigma_log 0.15), "
-                                f"{sc.tris.shape[0]} triangles, dt=1e-6 s, {args.model}, {args.precision}, "
-                                + (f"poured bed (settled {args.settle_steps} steps at dt=2e-5 s, e=0.1)"
-                                   if args.workload == "poured" else "loose lattice, v_sigma "
-                                   f"{args.v_sigma} m/s")),
+        "data": describe(args, sc)[0],
+        "config": {"workload": describe(args, sc)[1],
                    "n_particles": args.n, "n_triangles": int(sc.tris.shape[0]), "precision": args.precision,
                    "model": args.model, "l2": "inputs larger than L2 (state + lists > 129 MB per step)",
                    "parallelism": "replicas" if ws > 1 else "single GPU",
@@ -335,6 +351,21 @@ def active_only(sc):
                    history=None, hist_stride=0, active=None)
 
 
+def cpu_sample_scene(args, sc):
+    """The CPU path's share of the workload: all of it, except for the 10M
+    channel, whose full state does not fit the host path's fixed 100-slot
+    rows in memory: there the spheres of a tenth of the period (|x| < 5 cm),
+    with the whole mesh and the periodic x."""
+    from dataclasses import replace
+    sc = active_only(sc)
+    if args.workload != "channel" or sc.n <= 2_000_000:
+        return sc, ""
+    a = np.abs(sc.x[:, 0]) < 0.05
+    pick = lambda x: None if x is None else np.asarray(x)[a]
+    sub = replace(sc, x=sc.x[a], r=sc.r[a], m=sc.m[a], k=sc.k[a], eta=sc.eta[a], v=pick(sc.v), w=pick(sc.w))
+    return sub, f"; the {sub.n} spheres with |x| < 5 cm (a tenth of the period), whole mesh"
+
+
 def cpu_baseline(args, sc):
     """The reference algorithm's CPU implementation on the host cores, on a
     bounded sample of the same workload."""
@@ -343,7 +374,10 @@ def cpu_baseline(args, sc):
     except Exception as e:  # noqa: BLE001
         return {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                 "sample": f"unavailable: {e}"}
-    return port.time_sample(active_only(sc), budget_s=args.cpu_budget)
+    sub, note = cpu_sample_scene(args, sc)
+    out = port.time_sample(sub, budget_s=args.cpu_budget)
+    out["sample"] += note
+    return out
 
 
 def run_reference(args):
@@ -438,8 +472,8 @@ def main():
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=40)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--n", type=int, default=1_000_000)
-    ap.add_argument("--ntri", type=int, default=50_000)
+    ap.add_argument("--n", type=int, default=None, help="spheres (1M; 10M for the channel)")
+    ap.add_argument("--ntri", type=int, default=None, help="triangles (50k; 200k for the channel)")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--model", default="hertz_mindlin", choices=["linear", "hertz_mindlin"])
     ap.add_argument("--error-steps", type=int, default=1000)
@@ -452,7 +486,7 @@ def main():
     ap.add_argument("--v-sigma", type=float, default=0.5)
     ap.add_argument("--profile-iters", type=int, default=10)
     ap.add_argument("--e2e-steps", type=int, default=500)
-    ap.add_argument("--workload", default="poured", choices=["poured", "lattice", "batched"])
+    ap.add_argument("--workload", default="poured", choices=["poured", "lattice", "batched", "channel"])
     ap.add_argument("--n-scenes", type=int, default=256)
     ap.add_argument("--seq-steps", type=int, default=200)
     ap.add_argument("--autotune", action="store_true",
@@ -464,6 +498,11 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
+    channel = args.workload == "channel"
+    if args.n is None:
+        args.n = 10_000_000 if channel else 1_000_000
+    if args.ntri is None:
+        args.ntri = 200_000 if channel else 50_000
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "batched":

@@ -45,6 +45,7 @@ class Desc(C.Structure):
         ("youngs_modulus", C.c_double), ("poisson_ratio", C.c_double),
         ("restitution", C.c_double), ("rolling_friction", C.c_double),
         ("bvh_every_step", C.c_int), ("mixed_kernel", C.c_int), ("occupancy", C.c_int),
+        ("periodic_x", C.c_int),
     ]
 
 

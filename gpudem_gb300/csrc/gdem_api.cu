@@ -214,6 +214,24 @@ struct Impl : EngineBase {
         v.gz = d.g[2];
         v.minx = d.box_min[0]; v.miny = d.box_min[1]; v.minz = d.box_min[2];
         v.maxx = d.box_max[0]; v.maxy = d.box_max[1]; v.maxz = d.box_max[2];
+        v.per_x = d.periodic_x ? 1 : 0;
+        if (v.per_x) {
+            v.Lx = v.maxx - v.minx;
+            if (!(v.Lx > 0.)) return GDEM_ERR_ARG;
+            v.halfLx = 0.5 * v.Lx;
+            v.Lxh = (float)v.Lx;
+            v.Lxl = (float)(v.Lx - (double)v.Lxh);
+            v.halfLxf = (float)v.halfLx;
+            // a pair hi + lo below minx (at or above maxx) has hi <= minx
+            // (>= maxx) to within half an ulp of hi: test two ulps inside
+            float lo = (float)v.minx, hi = (float)v.maxx;
+            for (int k = 0; k < 2; k++) {
+                lo = nextafterf(lo, INFINITY);
+                hi = nextafterf(hi, -INFINITY);
+            }
+            v.perf[0] = lo;
+            v.perf[1] = hi;
+        }
         float xmax = 0.f;
         for (int k = 0; k < 3; k++) {
             v.boxf[k] = nextafterf((float)d.box_min[k], -INFINITY);
@@ -329,6 +347,15 @@ struct Impl : EngineBase {
         return GDEM_OK;
     }
 
+    // x moved into the period [minx, maxx) (periodic x; else unchanged)
+    double wrap_x(double x) const {
+        if (!v.per_x || !(x >= v.maxx || x < v.minx)) return x;
+        x -= v.Lx * floor((x - v.minx) / v.Lx);
+        if (x >= v.maxx) x -= v.Lx;
+        if (x < v.minx) x += v.Lx;
+        return x;
+    }
+
     int import_(const gdem_particles* p) override {
         CKE(cudaStreamSynchronize(st));
         destroy_graphs();
@@ -343,7 +370,7 @@ struct Impl : EngineBase {
         double rmax = 0.;
         for (int i = 0; i < n; i++) {
             const double r = p->r[i];
-            pos[i] = make_double4_32a(p->x[3 * i], p->x[3 * i + 1], p->x[3 * i + 2], r);
+            pos[i] = make_double4_32a(wrap_x(p->x[3 * i]), p->x[3 * i + 1], p->x[3 * i + 2], r);
             // derived per-particle constants in the operation order of
             // ParticleSystem.cu:294-333 (rsq = r*r, sqrtm, invm, moi = 2/5 m rsq)
             const double rsq = r * r;
@@ -400,6 +427,13 @@ struct Impl : EngineBase {
         v.thresh_sqf = (float)v.thresh_sq;
         v.invdx = v.invdy = v.invdz = 1. / cell;
         v.sizex = (int)ceil((v.maxx - v.minx) / cell) + 2;
+        if (v.per_x) {
+            // whole cells across the period, at least as wide as the cutoff
+            v.nxp = (int)floor(v.Lx / cell);
+            if (v.nxp < 3) return failv(err, GDEM_ERR_ARG, "periodic x: fewer than 3 cells across the period");
+            v.invdx = (double)v.nxp / v.Lx;
+            v.sizex = v.nxp + 2;
+        }
         v.sizey = (int)ceil((v.maxy - v.miny) / cell) + 2;
         v.sizez = (int)ceil((v.maxz - v.minz) / cell) + 2;
         if (v.sizex > 1024 || v.sizey > 1024 || v.sizez > 1024)
@@ -1016,6 +1050,12 @@ static int upload_mesh(gdem_handle* h, const std::vector<double>& vx, const std:
             d2 += e * e;
         }
         if (d2 > M.max_diag * M.max_diag) M.max_diag = std::sqrt(d2);
+    }
+    if (h->d.periodic_x) {
+        const double L = h->d.box_max[0] - h->d.box_min[0];
+        for (int t = 0; t < T; t++)
+            if (!(M.aabb_h[6 * t + 3] - M.aabb_h[6 * t] < 0.25 * L))
+                return fail(h, GDEM_ERR_ARG, "periodic x: a triangle is wider than a quarter period");
     }
     const int SCALE = (1 << 10) - 1;
     double inv[3];

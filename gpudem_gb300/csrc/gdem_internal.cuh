@@ -184,6 +184,12 @@ struct View {
     double gx, gy, gz;
     double minx, miny, minz, maxx, maxy, maxz;
     double invdx, invdy, invdz;
+    // periodic x: the period Lx = maxx - minx, its half, and nxp cells across
+    // it (cell x coordinates 1..nxp); in FP32 the period as a float pair
+    int per_x, nxp;
+    double Lx, halfLx;
+    float Lxh, Lxl, halfLxf;
+    float perf[2];                   // mixed mode: high-part x beyond which a centre may have left the period
     double skin, thresh_sq;
     float boxf[6];                   // mixed mode: box rounded outwards to FP32
     float nb_delta;                  // bound on |d_fp32 - d| of the list prefilter (m)
@@ -235,6 +241,44 @@ __host__ __device__ __forceinline__ uint32_t compact10(uint32_t v) {
 // (BoundingBox.cu:787-789).
 __device__ __forceinline__ int cell_coord(double x, double mn, double invd) {
     return (int)floor((x - mn) * invd) + 1;
+}
+
+// ---------------------------------------------------------------- periodic x
+// Cell x coordinate; with a periodic x every position lies in [minx, maxx)
+// and the coordinate is kept in 1..nxp against rounding at the top face.
+template <class T>
+__device__ __forceinline__ int cell_x(const View<T>& v, double x) {
+    int c = cell_coord(x, v.minx, v.invdx);
+    if (v.per_x) c = c < 1 ? 1 : (c > v.nxp ? v.nxp : c);
+    return c;
+}
+// Nearest-image x separation (the identity without a periodic x).
+template <class T>
+__device__ __forceinline__ double image_dx(const View<T>& v, double dx) {
+    if (v.per_x) {
+        if (dx > v.halfLx) dx -= v.Lx;
+        else if (dx < -v.halfLx) dx += v.Lx;
+    }
+    return dx;
+}
+template <class T>
+__device__ __forceinline__ float image_dxf(const View<T>& v, float dx) {
+    if (v.per_x) {
+        if (dx > v.halfLxf) dx -= v.Lxh;
+        else if (dx < -v.halfLxf) dx += v.Lxh;
+    }
+    return dx;
+}
+// x of a sphere centre moved to the image nearest the triangle whose first
+// corner is at x0 (triangles are narrower than a quarter period).
+template <class T>
+__device__ __forceinline__ double image_x_near(const View<T>& v, double x, double x0) {
+    if (v.per_x) {
+        const double d = x - x0;
+        if (d > v.halfLx) x -= v.Lx;
+        else if (d < -v.halfLx) x += v.Lx;
+    }
+    return x;
 }
 
 // ---------------------------------------------------------------- closest feature

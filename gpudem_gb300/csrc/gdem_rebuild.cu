@@ -212,7 +212,7 @@ __global__ void k_keys(View<T> v, int gated) {
     uint32_t key = kNoKey;
     if (S.rot[i].w != 0) {
         const double4_32a p = load_pos(S, i);
-        const int cx = cell_coord(p.x, v.minx, v.invdx);
+        const int cx = cell_x(v, p.x);
         const int cy = cell_coord(p.y, v.miny, v.invdy);
         const int cz = cell_coord(p.z, v.minz, v.invdz);
         key = morton3((uint32_t)cx, (uint32_t)cy, (uint32_t)cz);
@@ -398,7 +398,7 @@ __global__ void __launch_bounds__(kBlock) k_neighbors(View<T> v, int gated) {
             const double xi = pi.x, yi = pi.y, zi = pi.z, ri = pi.w;
             const double skin = v.skin;
             const float skinf = (float)v.skin, delta = v.nb_delta;
-            const int cx = cell_coord(xi, v.minx, v.invdx);
+            const int cx = cell_x(v, xi);
             const int cy = cell_coord(yi, v.miny, v.invdy);
             const int cz = cell_coord(zi, v.minz, v.invdz);
             int cand_pid[CAP];
@@ -411,15 +411,21 @@ __global__ void __launch_bounds__(kBlock) k_neighbors(View<T> v, int gated) {
                     const int yy = cy + sy;
                     if (yy < 0 || yy >= v.sizey) continue;
                     for (int sx = -1; sx <= 1; sx++) {
-                        const int xx = cx + sx;
-                        if (xx < 0 || xx >= v.sizex) continue;
+                        int xx = cx + sx;
+                        if (v.per_x) {
+                            // cells 1..nxp wrap around (nxp >= 3: no cell twice)
+                            if (xx < 1) xx += v.nxp;
+                            else if (xx > v.nxp) xx -= v.nxp;
+                        } else if (xx < 0 || xx >= v.sizex) {
+                            continue;
+                        }
                         const int cell = (v.sizey * zz + yy) * v.sizex + xx;
                         const int b = v.cell_start[cell], e = v.cell_end[cell];
                         for (int q = b; q < e; q++) {
                             const int j = v.reorder ? q : v.vals[0][q];
                             if (j == i) continue;
                             const float4 fj = PF[j];
-                            const float ex = fi.x - fj.x, ey = fi.y - fj.y, ez = fi.z - fj.z;
+                            const float ex = image_dxf(v, fi.x - fj.x), ey = fi.y - fj.y, ez = fi.z - fj.z;
                             const float dsqf = ex * ex + ey * ey + ez * ez;
                             const float Rf = fabsf(fi.w) + fabsf(fj.w) + skinf;
                             const float Rhi = Rf + delta, Rlo = Rf - delta;
@@ -427,7 +433,7 @@ __global__ void __launch_bounds__(kBlock) k_neighbors(View<T> v, int gated) {
                             bool inside = Rlo > 0.f && dsqf < Rlo * Rlo * 0.9999962f;  // surely inside
                             if (!inside) {
                                 const double4_32a pj = load_pos(S, j);
-                                const double dx = xi - pj.x;
+                                const double dx = image_dx(v, xi - pj.x);
                                 const double dy = yi - pj.y;
                                 const double dz = zi - pj.z;
                                 const double distsq = dx * dx + dy * dy + dz * dz;
@@ -492,41 +498,48 @@ __global__ void __launch_bounds__(kBlock) k_wall_lists(View<T> v, int gated) {
             v.nneiw[i] = 0;
         } else {
             const double4_32a pi = load_pos(S, i);
-            const double px = pi.x, py = pi.y, pz = pi.z;
+            const double py = pi.y, pz = pi.z;
             const double R = pi.w + v.skin;
             const double Rsq = R * R;
             int cand[CAP];
             bool overflow = false;
             int stack[kBvhStack];
-            int sp = 0;
-            stack[sp++] = v.bvh_root;
-            while (sp > 0) {
-                const int node = stack[--sp];
-                const BNode& B = v.bvh[node];
-                if (!sphere_aabb(px, py, pz, Rsq, B.lo, B.hi)) continue;
-                if (B.tri >= 0) {
-                    const int t = B.tri;
-                    const Feature f = closest_feature(px, py, pz, Rsq, v.tri[t]);
-                    if (f.dist < pi.w + v.skin) {
-                        if (count >= CAP) {
-                            overflow = true;
-                            continue;
+            // periodic x: a sphere within R of an x face also queries the mesh
+            // at its image one period away (no triangle is found twice: the
+            // mesh's triangles are narrower than a quarter period)
+            const int nimg = v.per_x && (pi.x + R > v.maxx || pi.x - R < v.minx) ? 2 : 1;
+            for (int img = 0; img < nimg; img++) {
+                const double px = img == 0 ? pi.x : (pi.x + R > v.maxx ? pi.x - v.Lx : pi.x + v.Lx);
+                int sp = 0;
+                stack[sp++] = v.bvh_root;
+                while (sp > 0) {
+                    const int node = stack[--sp];
+                    const BNode& B = v.bvh[node];
+                    if (!sphere_aabb(px, py, pz, Rsq, B.lo, B.hi)) continue;
+                    if (B.tri >= 0) {
+                        const int t = B.tri;
+                        const Feature f = closest_feature(px, py, pz, Rsq, v.tri[t]);
+                        if (f.dist < pi.w + v.skin) {
+                            if (count >= CAP) {
+                                overflow = true;
+                                continue;
+                            }
+                            int k = count;
+                            while (k > 0 && cand[k - 1] > t) {
+                                cand[k] = cand[k - 1];
+                                k--;
+                            }
+                            cand[k] = t;
+                            count++;
                         }
-                        int k = count;
-                        while (k > 0 && cand[k - 1] > t) {
-                            cand[k] = cand[k - 1];
-                            k--;
+                    } else {
+                        if (sp + 2 > kBvhStack) {
+                            atomicOr(&ctl->error, 0x10u);
+                            break;
                         }
-                        cand[k] = t;
-                        count++;
+                        stack[sp++] = B.left;
+                        stack[sp++] = B.right;
                     }
-                } else {
-                    if (sp + 2 > kBvhStack) {
-                        atomicOr(&ctl->error, 0x10u);
-                        break;
-                    }
-                    stack[sp++] = B.left;
-                    stack[sp++] = B.right;
                 }
             }
             if (overflow || count > v.wall_cap) atomicOr(&ctl->error, 0x2u);

@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(kBlock) k_stats(View<T> v, double* partials) {
             const int j = v.nei[(size_t)k * n + i];
             if (S.rot[j].w != 1) continue;
             const double4_32a q = load_pos(S, j);
-            const double dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+            const double dx = image_dx(v, p.x - q.x), dy = p.y - q.y, dz = p.z - q.z;
             const double R = r + q.w;
             const double d2 = dx * dx + dy * dy + dz * dz;
             if (d2 < R * R) acc[13] = fmax(acc[13], (R - sqrt(d2)) / (2. * r));
@@ -91,7 +91,7 @@ __global__ void k_keys_probe(View<T> v, uint32_t* out) {
     uint32_t key = kNoKey;
     if (S.rot[i].w == 1) {
         const double4_32a p = load_pos(S, i);
-        const int cx = cell_coord(p.x, v.minx, v.invdx);
+        const int cx = cell_x(v, p.x);
         const int cy = cell_coord(p.y, v.miny, v.invdy);
         const int cz = cell_coord(p.z, v.minz, v.invdz);
         key = morton3((uint32_t)cx, (uint32_t)cy, (uint32_t)cz);

@@ -180,7 +180,7 @@ __global__ void __launch_bounds__(kBlock) k_step(View<T> v, cudaGraphConditional
                 const V4 wj = A.rot[j];
                 if (wj.w != R(1)) continue;
                 const double4_32a pj = A.pos[j];
-                const R dx = (R)(xi - pj.x);
+                const R dx = (R)image_dx(v, xi - pj.x);
                 const R dy = (R)(yi - pj.y);
                 const R dz = (R)(zi - pj.z);
                 const R distsq = dx * dx + dy * dy + dz * dz;
@@ -300,7 +300,7 @@ __global__ void __launch_bounds__(kBlock) k_step(View<T> v, cudaGraphConditional
             const double rsq = rid * rid;
             for (int kk = 0; kk < nw; kk++) {
                 const int t = v.neiw[(size_t)kk * n + i];
-                const Feature f = closest_feature(xi, yi, zi, rsq, v.tri[t]);
+                const Feature f = closest_feature(image_x_near(v, xi, v.tri[t].v0[0]), yi, zi, rsq, v.tri[t]);
                 if (!(f.dist < rid)) continue;
                 if (f.hit != -1) {
                     // a vertex or edge shared by triangles acts once per step
@@ -422,13 +422,18 @@ __global__ void __launch_bounds__(kBlock) k_step(View<T> v, cudaGraphConditional
                 nyp = yi + nvy * dt;
                 nzp = zi + nvz * dt;
             }
+            // periodic x: back into the period (a step moves far less than one)
+            if (v.per_x) {
+                if (nxp >= v.maxx) nxp -= v.Lx;
+                else if (nxp < v.minx) nxp += v.Lx;
+            }
             const R aax = mx * invmoi, aay = my * invmoi, aaz = mz * invmoi;
             const R nwx = wi.x + aax * dt, nwy = wi.y + aay * dt, nwz = wi.z + aaz * dt;
             // ---------------- refresh test (shouldRefreshNeighborList, cpu_dem.cu:1529):
             // every particle active at the start of the step takes part
             {
                 const double4_32a rf = v.ref[i];
-                const double ex = nxp - rf.x, ey = nyp - rf.y, ez = nzp - rf.z;
+                const double ex = image_dx(v, nxp - rf.x), ey = nyp - rf.y, ez = nzp - rf.z;
                 const double d2 = ex * ex + ey * ey + ez * ez;
                 if (d2 > v.thresh_sq) refresh = true;
             }
@@ -437,7 +442,7 @@ __global__ void __launch_bounds__(kBlock) k_step(View<T> v, cudaGraphConditional
             // step (main.cu:312-316), so a particle leaving the box is marked 2:
             // still in this step's rebuild, inactive from the next step on.
             R status = R(1);
-            if (nxp < v.minx || nxp > v.maxx || nyp < v.miny || nyp > v.maxy || nzp < v.minz ||
+            if ((!v.per_x && (nxp < v.minx || nxp > v.maxx)) || nyp < v.miny || nyp > v.maxy || nzp < v.minz ||
                 nzp > v.maxz)
                 status = R(2);
             if (!(nxp == nxp && nyp == nyp && nzp == nzp)) {

@@ -142,12 +142,36 @@ __device__ __forceinline__ void two_diff(float a, float b, float& s, float& e) {
 struct PairGeom {
     float dx, dy, dz, Rs, num;
 };
-__device__ __forceinline__ PairGeom pair_geometry(float4 hi, float4 li, float4 hj, float4 lj) {
+// Periodic x in FP32: the period as a float pair L = Lh + Ll and its half.
+struct PerX {
+    int on;
+    float Lh, Ll, half;
+};
+template <class V>
+__device__ __forceinline__ PerX per_of(const V& v) {
+    return PerX{v.per_x, v.Lxh, v.Lxl, v.halfLxf};
+}
+// With a periodic x, the nearest image of the high-part x separation X:
+// X -/+ Lh is exact (Sterbenz: |X| lies between Lh/2 and 2 Lh), and the
+// period's low part joins the error term e.
+__device__ __forceinline__ void image_pair(const PerX& per, float& X, float& e) {
+    if (per.on) {
+        if (X > per.half) {
+            X = __fsub_rn(X, per.Lh);
+            e = __fsub_rn(e, per.Ll);
+        } else if (X < -per.half) {
+            X = __fadd_rn(X, per.Lh);
+            e = __fadd_rn(e, per.Ll);
+        }
+    }
+}
+__device__ __forceinline__ PairGeom pair_geometry(float4 hi, float4 li, float4 hj, float4 lj, const PerX& per) {
     PairGeom g;
     float X, Y, Z, eX, eY, eZ;
     two_diff(hi.x, hj.x, X, eX);
     two_diff(hi.y, hj.y, Y, eY);
     two_diff(hi.z, hj.z, Z, eZ);
+    image_pair(per, X, eX);
     eX = __fadd_rn(eX, __fsub_rn(li.x, lj.x));
     eY = __fadd_rn(eY, __fsub_rn(li.y, lj.y));
     eZ = __fadd_rn(eZ, __fsub_rn(li.z, lj.z));
@@ -175,9 +199,11 @@ __device__ __forceinline__ PairGeom pair_geometry(float4 hi, float4 li, float4 h
 // First contact test on the high parts alone (one gather per candidate):
 // 1 surely in contact, 0 surely not, -1 undecided (within `delta`, the bound
 // on what the low parts can move the distance, of touching).
-__device__ __forceinline__ int contact_hint(float4 hi, float4 hj, float delta) {
+__device__ __forceinline__ int contact_hint(float4 hi, float4 hj, float delta, const PerX& per) {
     if (!(hj.w > 0.f)) return 0;  // partner inactive or leaving the box
-    const float dx = hi.x - hj.x, dy = hi.y - hj.y, dz = hi.z - hj.z;
+    float dx = hi.x - hj.x;
+    const float dy = hi.y - hj.y, dz = hi.z - hj.z;
+    if (per.on) dx = dx > per.half ? dx - per.Lh : (dx < -per.half ? dx + per.Lh : dx);
     const float Rs = hi.w + hj.w;
     const float d2 = dx * dx + dy * dy + dz * dz;
     const float Rin = Rs - delta, Rout = Rs + delta;
@@ -188,8 +214,8 @@ __device__ __forceinline__ int contact_hint(float4 hi, float4 hj, float delta) {
 
 // The exact contact test (pair_geometry's num > 0) for the few candidates the
 // high parts leave undecided; kept out of line so the scan loop stays small.
-__device__ __noinline__ bool exact_contact(float4 hi, float4 li, float4 hj, float4 lj) {
-    return pair_geometry(hi, li, hj, lj).num > 0.f;
+__device__ __noinline__ bool exact_contact(float4 hi, float4 li, float4 hj, float4 lj, PerX per) {
+    return pair_geometry(hi, li, hj, lj, per).num > 0.f;
 }
 
 // a + b as an unevaluated pair (s, e), exactly
@@ -422,6 +448,21 @@ __device__ __forceinline__ Force6 pair_force(const View<Mixed>& v, const PairGeo
     return F;
 }
 
+// Sphere centre (ph + pl) moved to its x image nearest a triangle whose first
+// corner has high-part x x0h (periodic x; triangles are narrower than a
+// quarter period): the shift by -/+ L is formed as a float pair.
+__device__ __forceinline__ void wall_image(const PerX& per, float x0h, float3& ph, float3& pl) {
+    if (!per.on) return;
+    const float d = ph.x - x0h;
+    if (d > per.half || d < -per.half) {
+        const float sh = d > 0.f ? per.Lh : -per.Lh, sl = d > 0.f ? per.Ll : -per.Ll;
+        float s, e;
+        two_diff(ph.x, sh, s, e);
+        ph.x = s;
+        pl.x = __fadd_rn(__fsub_rn(pl.x, sl), e);
+    }
+}
+
 // Wall contacts of particle i from its wall list, in list order
 // (wall_collision_verlet, cpu_dem.cu:238), added to f and m.
 template <int MODEL, int WCAP>
@@ -437,6 +478,7 @@ __device__ __forceinline__ void wall_forces(const View<Mixed>& v, const PBank<Mi
     int vore[WCAP];
     int nvore = 0;
     const float3 ph = make_float3(hi.x, hi.y, hi.z), pl = make_float3(li.x, li.y, li.z);
+    const PerX per = per_of(v);
     // candidates within the FP32 error bound of touching go to the exact overlap
     const R rm = ri + v.wall_delta;
     const R rmsq = rm * rm;
@@ -454,7 +496,9 @@ __device__ __forceinline__ void wall_forces(const View<Mixed>& v, const PBank<Mi
             const float4* rec = reinterpret_cast<const float4*>(&v.trif[tt[q]]);
             const float4 a = __ldg(rec), b = __ldg(rec + 1), c = __ldg(rec + 2);
             // a = {v0h.xyz, v0l.x}, b = {v0l.yz, n.xy}, c = {n.z, ...}
-            const float ax = (ph.x - a.x) + (pl.x - a.w);
+            float3 qh = ph, ql = pl;
+            wall_image(per, a.x, qh, ql);
+            const float ax = (qh.x - a.x) + (ql.x - a.w);
             const float ay = (ph.y - a.y) + (pl.y - b.x);
             const float az = (ph.z - a.z) + (pl.z - b.y);
             const float dist = b.z * ax + b.w * ay + c.x * az;
@@ -464,9 +508,11 @@ __device__ __forceinline__ void wall_forces(const View<Mixed>& v, const PBank<Mi
             const int q = __ffs(near) - 1;
             near &= near - 1u;
             const int t = __ldg(&neiw[(size_t)(k0 + q) * n + i]);
-            const FeatureF f = closest_feature_f(ph, pl, rmsq, v.trif[t]);
+            float3 qh = ph, ql = pl;
+            wall_image(per, v.trif[t].v0h[0], qh, ql);
+            const FeatureF f = closest_feature_f(qh, ql, rmsq, v.trif[t]);
             if (!(f.dist < rm)) continue;
-            const R delmag = wall_overlap(ph, pl, ri, li.w, v.trif[t], v.trilo[t], f.kind, f.t);
+            const R delmag = wall_overlap(qh, ql, ri, li.w, v.trif[t], v.trilo[t], f.kind, f.t);
             if (!(delmag > 0.f)) continue;
         if (f.hit != -1) {
             bool dup = false;
@@ -594,6 +640,15 @@ __device__ __forceinline__ void integrate_one(const View<Mixed>& v, const SBank<
     nl.x += ex_;
     nl.y += ey_;
     nl.z += ez_;
+    // periodic x: back into the period.  Only a centre within two ulps of a
+    // face can have crossed it; those take the exact FP64 test and shift.
+    if (v.per_x && (nh.x > v.perf[1] || nh.x < v.perf[0])) {
+        double x = (double)nh.x + (double)nl.x;
+        if (x >= v.maxx) x -= v.Lx;
+        else if (x < v.minx) x += v.Lx;
+        nh.x = __double2float_rn(x);
+        nl.x = __double2float_rn(x - (double)nh.x);
+    }
     float nwx = o.wi.x, nwy = o.wi.y, nwz = o.wi.z;
     pair_add(nwx, wl.x, F.mx * invmoi * dt);
     pair_add(nwy, wl.y, F.my * invmoi * dt);
@@ -605,13 +660,13 @@ __device__ __forceinline__ void integrate_one(const View<Mixed>& v, const SBank<
     // leaves a margin of skin/2 to the list cutoff.  The flag is sticky: the
     // persistent kernels integrate many particles per thread.
     {
-        const R ex = nh.x - o.rh.x, ey = nh.y - o.rh.y, ez = nh.z - o.rh.z;
+        const R ex = image_dxf(v, nh.x - o.rh.x), ey = nh.y - o.rh.y, ez = nh.z - o.rh.z;
         if (ex * ex + ey * ey + ez * ez > v.thresh_sqf) refresh = true;
     }
-    // out of bounds (the box rounded outwards to FP32)
+    // out of bounds (the box rounded outwards to FP32; not in a periodic x)
     R status = 1.f;
-    if (nh.x < v.boxf[0] || nh.x > v.boxf[3] || nh.y < v.boxf[1] || nh.y > v.boxf[4] || nh.z < v.boxf[2] ||
-        nh.z > v.boxf[5])
+    if ((!v.per_x && (nh.x < v.boxf[0] || nh.x > v.boxf[3])) || nh.y < v.boxf[1] || nh.y > v.boxf[4] ||
+        nh.z < v.boxf[2] || nh.z > v.boxf[5])
         status = 2.f;
     if (!(nvx == nvx && nvy == nvy && nvz == nvz)) {
         err |= 0x20u;
@@ -642,6 +697,7 @@ __device__ __forceinline__ void step_one(const View<Mixed>& v, const SBank<Mixed
         return;
     }
     const int n = v.n;
+    const PerX per = per_of(v);
     const float4* __restrict__ Aposh = A.posh;
     const float4* __restrict__ Aposl = A.posl;
     const float4* __restrict__ Avel = A.vel;
@@ -670,8 +726,8 @@ __device__ __forceinline__ void step_one(const View<Mixed>& v, const SBank<Mixed
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             if (jj[q] < 0) continue;
-            const int h = contact_hint(hi, hj[q], v.nb_delta);
-            if (h > 0 || (h < 0 && exact_contact(hi, li, hj[q], __ldg(&Aposl[jj[q]])))) hit |= 1u << q;
+            const int h = contact_hint(hi, hj[q], v.nb_delta, per);
+            if (h > 0 || (h < 0 && exact_contact(hi, li, hj[q], __ldg(&Aposl[jj[q]]), per))) hit |= 1u << q;
         }
         while (hit) {
             const int q = __ffs(hit) - 1;
@@ -696,7 +752,7 @@ __device__ __forceinline__ void step_one(const View<Mixed>& v, const SBank<Mixed
                 cp.x = P.cx[h]; cp.y = P.cy[h]; cp.z = P.cz[h];
             }
             touched |= 1ull << slot;
-            const Force6 G = pair_force<MODEL>(v, pair_geometry(hi, li, hjq, ljq), ri, hjq.w, o.vi, o.wi, __ldg(&Avel[j]), __ldg(&Arot[j]),
+            const Force6 G = pair_force<MODEL>(v, pair_geometry(hi, li, hjq, ljq, per), ri, hjq.w, o.vi, o.wi, __ldg(&Avel[j]), __ldg(&Arot[j]),
                                                invmi, mt, sp, cp);
             F.fx += G.fx; F.fy += G.fy; F.fz += G.fz;
             F.mx += G.mx; F.my += G.my; F.mz += G.mz;
@@ -1004,6 +1060,7 @@ __global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<
     const int nsub = (n + 31) / 32;
     const int nei_rows = (n % 4 == 0) ? min(kNeiStageRows, v.nei_cap) : 0;
     const int hid_rows = (n % 4 == 0) ? min(kHidStageRows, v.hist_cap) : 0;
+    const PerX per = per_of(v);
     bool refresh = false;
     unsigned err = 0u;
     if (lane == 0) {
@@ -1081,8 +1138,8 @@ __global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<
 #pragma unroll
                 for (int q = 0; q < 4; q++) {
                     if (jj[q] < 0) continue;
-                    const int h = contact_hint(hi, hj[q], delta);
-                    if (h > 0 || (h < 0 && exact_contact(hi, li, hj[q], __ldg(&Aposl[jj[q]])))) hit |= 1u << q;
+                    const int h = contact_hint(hi, hj[q], delta, per);
+                    if (h > 0 || (h < 0 && exact_contact(hi, li, hj[q], __ldg(&Aposl[jj[q]]), per))) hit |= 1u << q;
                 }
                 if (k0 < 64)
                     hit_lo |= (unsigned long long)hit << k0;
@@ -1147,7 +1204,7 @@ __global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<
                     cp.x = P.cx[h]; cp.y = P.cy[h]; cp.z = P.cz[h];
                 }
                 const Mat mo = own_material<MODEL>(v, P, iow, hiw.w, viw.w);
-                const Force6 G = pair_force<MODEL>(v, pair_geometry(hiw, liw, hjq, ljq), hiw.w, hjq.w, viw, wiw, vj, wj,
+                const Force6 G = pair_force<MODEL>(v, pair_geometry(hiw, liw, hjq, ljq, per), hiw.w, hjq.w, viw, wiw, vj, wj,
                                                    viw.w, mo, sp, cp);
                 P.hx[h] = sp.x; P.hy[h] = sp.y; P.hz[h] = sp.z;
                 P.cx[h] = cp.x; P.cy[h] = cp.y; P.cz[h] = cp.z;

@@ -67,6 +67,8 @@ class Engine:
         d.mu = scene.mu
         for k in range(3):
             d.g[k] = float(scene.g[k])
+        if box is None and scene.box is not None:
+            box = scene.box
         lo, hi = box if box is not None else box_limits(scene.tris, scene.inlet_lo, scene.inlet_hi)
         self.box_lo, self.box_hi = np.asarray(lo, np.float64), np.asarray(hi, np.float64)
         for k in range(3):
@@ -82,6 +84,7 @@ class Engine:
         d.bvh_every_step = 1 if bvh_every_step else 0
         d.mixed_kernel = int(mixed_kernel)
         d.occupancy = int(occupancy)
+        d.periodic_x = 1 if scene.periodic_x else 0
         self.desc = d
         h = C.c_void_p()
         _lib.check(self.L.gdem_create(C.byref(d), C.byref(h)), None, "gdem_create")

@@ -155,9 +155,13 @@ def helical_chute_mesh(radius=0.3, pitch=0.1, turns=2.0, width=0.12, wall=0.05,
     return np.asarray(tris, dtype=np.float64)
 
 
-def corrugated_floor_mesh(length=1.0, width=0.2, amp=0.003, n_target=200_000, seed=5) -> np.ndarray:
+def corrugated_floor_mesh(length=1.0, width=0.2, amp=0.003, n_target=200_000, seed=5,
+                          periodic=False) -> np.ndarray:
     """Floor of a channel along x with seeded sinusoidal bumps of amplitude
-    `amp`, triangulated to about `n_target` triangles (a regular grid of quads)."""
+    `amp`, triangulated to about `n_target` triangles (a regular grid of quads)
+    over x in [-length/2, length/2], z in [-width/2, width/2].  `periodic`
+    rounds the x wavenumber to a whole number of waves per length, so the
+    floor continues across x = -length/2 ~ length/2."""
     rng = np.random.default_rng(seed)
     nx = int(math.sqrt(n_target / 2 * length / width))
     nz = max(1, int(n_target / 2 / nx))
@@ -166,6 +170,8 @@ def corrugated_floor_mesh(length=1.0, width=0.2, amp=0.003, n_target=200_000, se
     X, Z = np.meshgrid(x, z, indexing="ij")
     k1, k2 = rng.uniform(20, 60, 2)
     p1, p2 = rng.uniform(0, 2 * math.pi, 2)
+    if periodic:
+        k1 = 2 * math.pi / length * max(1, round(k1 * length / (2 * math.pi)))
     Y = amp * np.sin(k1 * X + p1) * np.cos(k2 * Z + p2)
     P = np.stack([X, Y, Z], -1)
     a = P[:-1, :-1].reshape(-1, 3)
@@ -277,6 +283,10 @@ class Scene:
     # per-particle Hertz-Mindlin friction and restitution (packed scenes)
     mu_p: np.ndarray | None = None
     e_p: np.ndarray | None = None
+    # box limits (lo, hi) to use instead of the reference's rule from the mesh
+    # and inlet; with periodic_x its x extent is the period
+    box: tuple | None = None
+    periodic_x: bool = False
 
     @property
     def n(self) -> int:
@@ -538,6 +548,58 @@ def pack_scenes(scenes: list, gap=None):
                    mu_p=cat(lambda s, sc: np.full(sc.n, sc.mu)), e_p=cat(lambda s, sc: np.full(sc.n, sc.e)),
                    name=f"packed-{len(scenes)}-scenes")
     return packed, offs, starts
+
+
+def side_wall_mesh(length, z, y0, y1, pieces=8) -> np.ndarray:
+    """Vertical wall z = const over x in [-length/2, length/2], y in [y0, y1],
+    as `pieces` quads along x (two triangles each)."""
+    xs = np.linspace(-0.5 * length, 0.5 * length, pieces + 1)
+    tris = []
+    for a, b in zip(xs[:-1], xs[1:]):
+        tris += _quad(np.array([a, y0, z]), np.array([b, y0, z]), np.array([b, y1, z]), np.array([a, y1, z]))
+    return np.asarray(tris, np.float64)
+
+
+def config5_periodic_channel(n=10_000_000, seed=5, length=1.0, width=0.5, n_tri=200_000, amp=0.003,
+                             v_drift=0.0, v_sigma=0.1, dt=1e-6) -> Scene:
+    """Spheres in a channel periodic in x: bidisperse radii 1.0 / 1.5 mm at
+    70 / 30 (seeded), a floor of about `n_tri` triangles with seeded
+    sinusoidal corrugation of amplitude `amp` (a whole number of waves per
+    period), flat side walls at z = +-width/2 cut into pieces narrower than a
+    quarter period, open top.  The spheres start on a jittered lattice above
+    the floor with seeded Gaussian velocities (`v_sigma`) plus `v_drift` along
+    x.  Hertz-Mindlin E=5e6 Pa, nu=0.3, e=0.5, mu=0.5, rolling friction 0.05.
+    The box's x extent [-length/2, length/2) is the period."""
+    rng = np.random.default_rng(seed)
+    radii = np.where(rng.random(n) < 0.7, 1.0e-3, 1.5e-3)
+    rmax = float(radii.max())
+    floor = corrugated_floor_mesh(length, width, amp, n_tri - 32, seed, periodic=True)
+    a = 2.0 * rmax * 1.05
+    nxl = int(math.floor(length / a))
+    nzl = int(math.floor((width - 2 * rmax - 2e-3) / a))
+    per_layer = nxl * nzl
+    layers = int(math.ceil(n / per_layer))
+    y_top = amp + 2e-3 + rmax + layers * a
+    walls = np.concatenate([side_wall_mesh(length, -0.5 * width, -amp - 0.01, y_top + 0.01),
+                            side_wall_mesh(length, 0.5 * width, -amp - 0.01, y_top + 0.01)])
+    tris = np.concatenate([floor, walls])
+    sites = rng.permutation(per_layer * layers)[:n]
+    ix = sites % nxl
+    iz = (sites // nxl) % nzl
+    iy = sites // per_layer
+    x = np.stack([-0.5 * length + (ix + 0.5) * (length / nxl),
+                  amp + 2e-3 + rmax + iy * a,
+                  -0.5 * width + rmax + 1e-3 + (iz + 0.5) * a], 1)
+    x += (rng.random((n, 3)) - 0.5) * (0.04 * rmax)
+    m = sphere_mass(2500.0, radii)
+    k = np.full(n, stiffness_from_E(5e6, 1e-3))
+    v = rng.normal(0.0, v_sigma, (n, 3)) if v_sigma > 0 else np.zeros((n, 3))
+    v[:, 0] += v_drift
+    lo = np.array([-0.5 * length, -amp - 0.02, -0.5 * width - 0.01])
+    hi = np.array([0.5 * length, y_top + 0.05, 0.5 * width + 0.01])
+    return Scene(x=x, r=radii, m=m, k=k, eta=eta_const(k, 0.5), mu=0.5, dt=dt, tris=tris,
+                 inlet_lo=lo, inlet_hi=hi, v=v, E=5e6, nu=0.3, e=0.5, mu_roll=0.05,
+                 box=(lo, hi), periodic_x=True, name=f"periodic-channel-{n}")
 
 
 # --------------------------------------------------------------------------- physics checks

@@ -84,6 +84,13 @@ typedef struct gdem_desc {
      * 0 default (warp-cooperative), 1 warp-cooperative, 2 warp-staged, 3 one thread per particle */
     int mixed_kernel;
     int occupancy;          /* resident CTAs per SM its registers are sized for; 0: default (4..6 / 2..3) */
+    /* 1: periodic in x.  [box_min[0], box_max[0]) is one period L: a particle
+     * leaving through one x face re-enters through the other, and particle pairs
+     * and particle-triangle pairs interact through the nearest x image.  The
+     * mesh must lie in the period with no triangle wider than L/4 in x; cells
+     * are L/floor(L/cell_size) wide in x (at least 3 of them).  No reference
+     * counterpart (the reference's box only deactivates what leaves it). */
+    int periodic_x;
 } gdem_desc;
 
 /* Particle arrays in the reference layout (memberList/ParticleSystemMember_common.def).

@@ -123,6 +123,10 @@ struct Scene {
     std::vector<int> nei, nnei, neiw, nneiw;
     // box
     double bmin[3], bmax[3], dx, inv, skin, thresh, threshSq;
+    // periodic x (an extension; the reference has none): [bmin[0], bmax[0])
+    // is one period L, nxp cells of 1/invx across it
+    int per_x = 0, nxp = 0;
+    double L = 0., halfL = 0., invx = 0.;
     int size[3], ncells;
     std::vector<int> pNum, pStart, pList, cellOff;
     Mesh mesh;
@@ -303,15 +307,23 @@ void build_bvh(Bvh& B, const Mesh& M) {
     B.nodes = count;
 }
 
-// closest feature of triangle t to particle i within radius^2 rsq
+// nearest-image x separation with a periodic x
+inline double image_dx(const Scene& S, double dx) {
+    if (S.per_x) {
+        if (dx > S.halfL) dx -= S.L;
+        else if (dx < -S.halfL) dx += S.L;
+    }
+    return dx;
+}
+
+// closest feature of triangle t to the centre p within radius^2 rsq
 // (dist_triangle cpu_dem.cu:12-205; dist_triangle_neighbor BVH.cu:44-238)
-Feature feature(const Scene& S, int i, int t, double rsq) {
+Feature feature_at(const Scene& S, V3 p, int t, double rsq) {
     const Mesh& M = S.mesh;
     Feature res;
     res.n = {0., 0., 0.};
     res.dist = 1.e10;
     res.hit = -2;
-    const V3 p{S.x[3 * i], S.x[3 * i + 1], S.x[3 * i + 2]};
     double dist = 0.;
     dist += M.nx[t] * p.x;
     dist += M.ny[t] * p.y;
@@ -374,8 +386,26 @@ Feature feature(const Scene& S, int i, int t, double rsq) {
     return res;
 }
 
+// ... of particle i, at its x image nearest the triangle's first corner
+// with a periodic x (triangles are narrower than a quarter period)
+Feature feature(const Scene& S, int i, int t, double rsq) {
+    double px = S.x[3 * i];
+    if (S.per_x) {
+        const double d = px - S.mesh.mx[S.mesh.i0[t]];
+        if (d > S.halfL) px -= S.L;
+        else if (d < -S.halfL) px += S.L;
+    }
+    return feature_at(S, V3{px, S.x[3 * i + 1], S.x[3 * i + 2]}, t, rsq);
+}
+
 // ------------------------------------------------------------------ cells and lists
-inline int cell_of(const Scene& S, double x, int a) { return (int)floor((x - S.bmin[a]) * S.inv) + 1; }
+inline int cell_of(const Scene& S, double x, int a) {
+    if (a == 0 && S.per_x) {
+        const int c = (int)floor((x - S.bmin[0]) * S.invx) + 1;
+        return c < 1 ? 1 : (c > S.nxp ? S.nxp : c);
+    }
+    return (int)floor((x - S.bmin[a]) * S.inv) + 1;
+}
 
 // canonical CSR: cell-id order, ascending index within a cell (update_pList, BoundingBox.cu:839)
 void plist(Scene& S) {
@@ -427,15 +457,21 @@ bool build_lists(Scene& S) {
                     // A particle leaving the box this step is still listed
                     // (main.cu:312-316) and may sit in a ghost cell; the
                     // reference then indexes outside its cell arrays.  Cells
-                    // outside the grid hold nobody, so they are skipped.
-                    if (cx + sx < 0 || cx + sx >= S.size[0] || cy + sy < 0 || cy + sy >= S.size[1] ||
-                        cz + sz < 0 || cz + sz >= S.size[2])
+                    // outside the grid hold nobody, so they are skipped.  A
+                    // periodic x wraps cells 1..nxp around.
+                    int xx = cx + sx;
+                    if (S.per_x) {
+                        if (xx < 1) xx += S.nxp;
+                        else if (xx > S.nxp) xx -= S.nxp;
+                    } else if (xx < 0 || xx >= S.size[0]) {
                         continue;
-                    const int c = (S.size[1] * (cz + sz) + cy + sy) * S.size[0] + cx + sx;
+                    }
+                    if (cy + sy < 0 || cy + sy >= S.size[1] || cz + sz < 0 || cz + sz >= S.size[2]) continue;
+                    const int c = (S.size[1] * (cz + sz) + cy + sy) * S.size[0] + xx;
                     for (int q = S.pStart[c]; q < S.pStart[c] + S.pNum[c]; q++) {
                         const int j = S.pList[q];
                         if (i == j || S.active[j] != 1) continue;
-                        const V3 del{S.x[3 * i] - S.x[3 * j], S.x[3 * i + 1] - S.x[3 * j + 1],
+                        const V3 del{image_dx(S, S.x[3 * i] - S.x[3 * j]), S.x[3 * i + 1] - S.x[3 * j + 1],
                                      S.x[3 * i + 2] - S.x[3 * j + 2]};
                         const double dsq = dot(del, del);
                         const double R = S.r[i] + S.r[j] + skin;
@@ -463,9 +499,16 @@ bool build_lists(Scene& S) {
             const double R = S.r[i] + skin;
             const double Rsq = R * R;
             std::vector<int> stack;
-            stack.push_back(0);
             int nn = 0;
-            const double px = S.x[3 * i], py = S.x[3 * i + 1], pz = S.x[3 * i + 2];
+            const double py = S.x[3 * i + 1], pz = S.x[3 * i + 2];
+            // periodic x: a sphere within R of an x face also queries at its
+            // image one period away
+            const double x0 = S.x[3 * i];
+            const int nimg = S.per_x && (x0 + R > S.bmax[0] || x0 - R < S.bmin[0]) ? 2 : 1;
+            for (int img = 0; img < nimg; img++) {
+            const double px = img == 0 ? x0 : (x0 + R > S.bmax[0] ? x0 - S.L : x0 + S.L);
+            stack.clear();
+            stack.push_back(0);
             while (!stack.empty()) {
                 const int node = stack.back();
                 stack.pop_back();
@@ -479,7 +522,7 @@ bool build_lists(Scene& S) {
                 if (!((dx * dx + dy * dy + dz * dz) <= Rsq)) continue;
                 if (S.bvh.tri[node] >= 0) {
                     const int t = S.bvh.tri[node];
-                    const Feature f = feature(S, i, t, Rsq);
+                    const Feature f = feature_at(S, V3{px, py, pz}, t, Rsq);
                     if (f.dist < S.r[i] + skin) {
                         if (nn < K) S.neiw[(size_t)i * K + nn] = t;
                         nn++;
@@ -488,6 +531,7 @@ bool build_lists(Scene& S) {
                     stack.push_back(S.bvh.left[node]);
                     stack.push_back(S.bvh.right[node]);
                 }
+            }
             }
             if (nn > K) {
                 ok = false;
@@ -677,7 +721,8 @@ bool step(Scene& S) {
         for (int q = 0; q < S.nnei[i]; q++) {
             const int j = S.nei[(size_t)i * K + q];
             if (S.active[j] != 1) continue;
-            const V3 del{S.x[3 * i] - S.x[3 * j], S.x[3 * i + 1] - S.x[3 * j + 1], S.x[3 * i + 2] - S.x[3 * j + 2]};
+            const V3 del{image_dx(S, S.x[3 * i] - S.x[3 * j]), S.x[3 * i + 1] - S.x[3 * j + 1],
+                         S.x[3 * i + 2] - S.x[3 * j + 2]};
             const double dsq = dot(del, del);
             const double R = S.r[i] + S.r[j];
             if (dsq < R * R) {
@@ -726,6 +771,10 @@ bool step(Scene& S) {
             S.v[3 * i + a] += S.a[3 * i + a] * S.dt;
             S.x[3 * i + a] += S.v[3 * i + a] * S.dt;
         }
+        if (S.per_x) {
+            if (S.x[3 * i] >= S.bmax[0]) S.x[3 * i] -= S.L;
+            else if (S.x[3 * i] < S.bmin[0]) S.x[3 * i] += S.L;
+        }
         for (int a = 0; a < 3; a++) {
             S.anga[3 * i + a] = S.mom[3 * i + a] * S.invmoi[i];
             S.w[3 * i + a] += S.anga[3 * i + a] * S.dt;
@@ -735,14 +784,15 @@ bool step(Scene& S) {
     bool refresh = false;
     for (int i = 0; i < N && !refresh; i++) {
         if (S.active[i] != 1) continue;
-        const V3 del{S.x[3 * i] - S.refx[i], S.x[3 * i + 1] - S.refy[i], S.x[3 * i + 2] - S.refz[i]};
+        const V3 del{image_dx(S, S.x[3 * i] - S.refx[i]), S.x[3 * i + 1] - S.refy[i], S.x[3 * i + 2] - S.refz[i]};
         if (dot(del, del) > S.threshSq) refresh = true;
     }
     if (refresh) ok = build_lists(S);
     for (int i = 0; i < N; i++) {
         if (S.active[i] == 0) continue;
         const double X = S.x[3 * i], Y = S.x[3 * i + 1], Z = S.x[3 * i + 2];
-        if (X < S.bmin[0] || X > S.bmax[0] || Y < S.bmin[1] || Y > S.bmax[1] || Z < S.bmin[2] || Z > S.bmax[2])
+        if ((!S.per_x && (X < S.bmin[0] || X > S.bmax[0])) || Y < S.bmin[1] || Y > S.bmax[1] || Z < S.bmin[2] ||
+            Z > S.bmax[2])
             S.active[i] = 0;
     }
     S.steps++;
@@ -756,7 +806,8 @@ extern "C" {
 void* orc_create(int N, const double* x, const double* v, const double* w, const double* r, const double* m,
                  const double* k, const double* eta, double mu, double dt, const double* g, int nTri,
                  const double* tris, const int* files, int nfiles, const double* bmin, const double* bmax,
-                 double skin, double thresh, int model, double E, double nu, double e, double mu_roll) {
+                 double skin, double thresh, int model, double E, double nu, double e, double mu_roll,
+                 int periodic_x) {
     Scene* S = new Scene();
     S->N = N;
     S->dt = dt;
@@ -820,6 +871,26 @@ void* orc_create(int N, const double* x, const double* v, const double* w, const
     S->thresh = skin > 0 ? thresh : rmax * 0.5;
     S->threshSq = S->thresh * S->thresh;
     for (int a = 0; a < 3; a++) S->size[a] = (int)ceil((S->bmax[a] - S->bmin[a]) / S->dx) + 2;
+    if (periodic_x) {
+        S->per_x = 1;
+        S->L = S->bmax[0] - S->bmin[0];
+        S->halfL = 0.5 * S->L;
+        S->nxp = (int)floor(S->L / S->dx);
+        if (S->nxp < 3) {
+            delete S;
+            return nullptr;
+        }
+        S->invx = (double)S->nxp / S->L;
+        S->size[0] = S->nxp + 2;
+        for (int i = 0; i < N; i++) {
+            double& X = S->x[3 * i];
+            if (X >= S->bmax[0] || X < S->bmin[0]) {
+                X -= S->L * floor((X - S->bmin[0]) / S->L);
+                if (X >= S->bmax[0]) X -= S->L;
+                if (X < S->bmin[0]) X += S->L;
+            }
+        }
+    }
     S->ncells = S->size[0] * S->size[1] * S->size[2];
     S->pNum.assign(S->ncells, 0);
     S->pStart.assign(S->ncells, 0);

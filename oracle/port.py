@@ -27,7 +27,7 @@ def lib():
         L.orc_create.restype = vp
         L.orc_create.argtypes = [C.c_int, vp, vp, vp, vp, vp, vp, vp, C.c_double, C.c_double, vp, C.c_int, vp,
                                  vp, C.c_int, vp, vp, C.c_double, C.c_double, C.c_int, C.c_double, C.c_double,
-                                 C.c_double, C.c_double]
+                                 C.c_double, C.c_double, C.c_int]
         L.orc_destroy.argtypes = [vp]
         L.orc_step.argtypes = [vp, C.c_int]
         L.orc_step.restype = C.c_int
@@ -65,6 +65,8 @@ class OracleScene:
         L = lib()
         self.sc = sc
         self.N = sc.n
+        if box is None and sc.box is not None:
+            box = sc.box
         lo, hi = box if box is not None else box_limits(sc.tris, sc.inlet_lo, sc.inlet_hi)
         self._keep = [np.ascontiguousarray(a, np.float64) for a in (
             np.asarray(sc.x).ravel(), None if sc.v is None else np.asarray(sc.v).ravel(),
@@ -84,7 +86,9 @@ class OracleScene:
                               _vp(arrs[3]), float(sc.mu), float(sc.dt), _vp(arrs[4]), self.nTri, _vp(tris),
                               _vp(fl), 0 if fl is None else fl.size, _vp(lo), _vp(hi), float(sc.skin),
                               float(sc.refresh), {"linear": 0, "hertz_mindlin": 1}[model], float(sc.E),
-                              float(sc.nu), float(sc.e), float(sc.mu_roll))
+                              float(sc.nu), float(sc.e), float(sc.mu_roll), 1 if sc.periodic_x else 0)
+        if not self.h:
+            raise ValueError("oracle: bad scene (a periodic x needs at least 3 cells across the period)")
 
     def step(self, n=1):
         rc = lib().orc_step(self.h, int(n))
