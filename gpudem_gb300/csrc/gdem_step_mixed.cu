@@ -147,9 +147,11 @@ struct PerX {
     int on;
     float Lh, Ll, half;
 };
-template <class V>
+// PER: the kernel is compiled for a periodic x (false: every periodic branch
+// folds away at compile time)
+template <bool PER, class V>
 __device__ __forceinline__ PerX per_of(const V& v) {
-    return PerX{v.per_x, v.Lxh, v.Lxl, v.halfLxf};
+    return PER ? PerX{v.per_x, v.Lxh, v.Lxl, v.halfLxf} : PerX{0, 0.f, 0.f, 0.f};
 }
 // With a periodic x, the nearest image of the high-part x separation X:
 // X -/+ Lh is exact (Sterbenz: |X| lies between Lh/2 and 2 Lh), and the
@@ -465,7 +467,7 @@ __device__ __forceinline__ void wall_image(const PerX& per, float x0h, float3& p
 
 // Wall contacts of particle i from its wall list, in list order
 // (wall_collision_verlet, cpu_dem.cu:238), added to f and m.
-template <int MODEL, int WCAP>
+template <int MODEL, int WCAP, bool PER>
 __device__ __forceinline__ void wall_forces(const View<Mixed>& v, const PBank<Mixed>& P, int i, int nw, int ncw,
                                             float4 hi, float4 li, float4 vi, float4 wi, float invmi, const Mat& mt,
                                             Force6& F, unsigned& err) {
@@ -478,7 +480,7 @@ __device__ __forceinline__ void wall_forces(const View<Mixed>& v, const PBank<Mi
     int vore[WCAP];
     int nvore = 0;
     const float3 ph = make_float3(hi.x, hi.y, hi.z), pl = make_float3(li.x, li.y, li.z);
-    const PerX per = per_of(v);
+    const PerX per = per_of<PER>(v);
     // candidates within the FP32 error bound of touching go to the exact overlap
     const R rm = ri + v.wall_delta;
     const R rmsq = rm * rm;
@@ -618,9 +620,11 @@ __device__ __forceinline__ void freeze_one(const View<Mixed>& v, const SBank<Mix
 // Symplectic Euler (cpu_dem.cu:1622-1652) on the float pairs of position,
 // velocity and spin, so their many small increments do not round away; the
 // refresh and out-of-box tests; the new state into bank s^1.
+template <bool PER>
 __device__ __forceinline__ void integrate_one(const View<Mixed>& v, const SBank<Mixed>& B, int i, const Own& o,
                                               float invmoi, const Force6& F, bool& refresh, unsigned& err) {
     using R = float;
+    const PerX per = per_of<PER>(v);
     const R dt = v.dtf;
     const R invmi = o.vi.w;
     float4 vl = o.vl, wl = o.wl;
@@ -642,7 +646,7 @@ __device__ __forceinline__ void integrate_one(const View<Mixed>& v, const SBank<
     nl.z += ez_;
     // periodic x: back into the period.  Only a centre within two ulps of a
     // face can have crossed it; those take the exact FP64 test and shift.
-    if (v.per_x && (nh.x > v.perf[1] || nh.x < v.perf[0])) {
+    if (per.on && (nh.x > v.perf[1] || nh.x < v.perf[0])) {
         double x = (double)nh.x + (double)nl.x;
         if (x >= v.maxx) x -= v.Lx;
         else if (x < v.minx) x += v.Lx;
@@ -660,12 +664,14 @@ __device__ __forceinline__ void integrate_one(const View<Mixed>& v, const SBank<
     // leaves a margin of skin/2 to the list cutoff.  The flag is sticky: the
     // persistent kernels integrate many particles per thread.
     {
-        const R ex = image_dxf(v, nh.x - o.rh.x), ey = nh.y - o.rh.y, ez = nh.z - o.rh.z;
+        R ex = nh.x - o.rh.x;
+        if (per.on) ex = ex > per.half ? ex - per.Lh : (ex < -per.half ? ex + per.Lh : ex);
+        const R ey = nh.y - o.rh.y, ez = nh.z - o.rh.z;
         if (ex * ex + ey * ey + ez * ez > v.thresh_sqf) refresh = true;
     }
     // out of bounds (the box rounded outwards to FP32; not in a periodic x)
     R status = 1.f;
-    if ((!v.per_x && (nh.x < v.boxf[0] || nh.x > v.boxf[3])) || nh.y < v.boxf[1] || nh.y > v.boxf[4] ||
+    if ((!per.on && (nh.x < v.boxf[0] || nh.x > v.boxf[3])) || nh.y < v.boxf[1] || nh.y > v.boxf[4] ||
         nh.z < v.boxf[2] || nh.z > v.boxf[5])
         status = 2.f;
     if (!(nvx == nvx && nvy == nvy && nvz == nvz)) {
@@ -686,7 +692,7 @@ __device__ __forceinline__ void integrate_one(const View<Mixed>& v, const SBank<
 // One particle's step, one thread: particle contacts in row order (the row
 // read four entries at a time so their gathers are in flight together), wall
 // contacts, integration.  Writes bank s^1 and the history.
-template <int MODEL, int WCAP>
+template <int MODEL, int WCAP, bool PER>
 __device__ __forceinline__ void step_one(const View<Mixed>& v, const SBank<Mixed>& A, const SBank<Mixed>& B,
                                          const PBank<Mixed>& P, int i, const Own& o, bool& refresh, unsigned& err,
                                          const int* nei_s = nullptr, int nei_s_rows = 0) {
@@ -697,7 +703,7 @@ __device__ __forceinline__ void step_one(const View<Mixed>& v, const SBank<Mixed
         return;
     }
     const int n = v.n;
-    const PerX per = per_of(v);
+    const PerX per = per_of<PER>(v);
     const float4* __restrict__ Aposh = A.posh;
     const float4* __restrict__ Aposl = A.posl;
     const float4* __restrict__ Avel = A.vel;
@@ -761,12 +767,12 @@ __device__ __forceinline__ void step_one(const View<Mixed>& v, const SBank<Mixed
         }
     }
     P.nc[i] = surviving(touched, nc);
-    wall_forces<MODEL, WCAP>(v, P, i, o.nw, o.ncw, hi, li, o.vi, o.wi, invmi, mt, F, err);
-    integrate_one(v, B, i, o, mt.invmoi, F, refresh, err);
+    wall_forces<MODEL, WCAP, PER>(v, P, i, o.nw, o.ncw, hi, li, o.vi, o.wi, invmi, mt, F, err);
+    integrate_one<PER>(v, B, i, o, mt.invmoi, F, refresh, err);
 }
 
 // One thread per particle, state loaded straight from HBM.
-template <int MODEL, int WCAP, int MINB>
+template <int MODEL, int WCAP, int MINB, bool PER>
 __global__ void __launch_bounds__(kBlock, MINB) k_step_mixed(View<Mixed> v, cudaGraphConditionalHandle cond,
                                                             int use_cond) {
     Ctl* ctl = v.ctl;
@@ -790,7 +796,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_step_mixed(View<Mixed> v, cuda
         o.nw = __ldg(&v.nneiw[i]);
         o.nc = P.nc[i];
         o.ncw = P.ncw[i];
-        step_one<MODEL, WCAP>(v, A, B, P, i, o, refresh, err);
+        step_one<MODEL, WCAP, PER>(v, A, B, P, i, o, refresh, err);
     }
     step_epilogue(ctl, s, refresh, err, cond, use_cond);
 }
@@ -878,7 +884,7 @@ __device__ __forceinline__ void issue_sub(const View<Mixed>& v, const SBank<Mixe
     for (int k = 0; k < nei_rows; k++) bulk_g2s(st->nei[k], v.nei + (size_t)k * v.n + base, b4, bar);
 }
 
-template <int MODEL, int WCAP>
+template <int MODEL, int WCAP, bool PER>
 __global__ void __launch_bounds__(kBlock, 2) k_step_mixed_wtma(View<Mixed> v, cudaGraphConditionalHandle cond,
                                                               int use_cond) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -935,7 +941,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_step_mixed_wtma(View<Mixed> v, cu
             o.nw = S.nneiw[lane];
             o.nc = S.nc[lane];
             o.ncw = S.ncw[lane];
-            step_one<MODEL, WCAP>(v, A, B, P, i, o, refresh, err, &S.nei[0][lane], nei_rows);
+            step_one<MODEL, WCAP, PER>(v, A, B, P, i, o, refresh, err, &S.nei[0][lane], nei_rows);
         }
         __syncwarp();
     }
@@ -1036,7 +1042,7 @@ __device__ __forceinline__ int find_slot_staged(int* hid_s, int rows, int* hid, 
     return q;
 }
 
-template <int MODEL, int WCAP, int MINB>
+template <int MODEL, int WCAP, int MINB, bool PER>
 __global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<Mixed> v, cudaGraphConditionalHandle cond,
                                                                     int use_cond) {
     using R = float;
@@ -1060,7 +1066,7 @@ __global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<
     const int nsub = (n + 31) / 32;
     const int nei_rows = (n % 4 == 0) ? min(kNeiStageRows, v.nei_cap) : 0;
     const int hid_rows = (n % 4 == 0) ? min(kHidStageRows, v.hist_cap) : 0;
-    const PerX per = per_of(v);
+    const PerX per = per_of<PER>(v);
     bool refresh = false;
     unsigned err = 0u;
     if (lane == 0) {
@@ -1237,11 +1243,11 @@ __global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<
             o.vi = S.vel[lane];
             const R invmi = o.vi.w;
             const Mat mt = own_material<MODEL>(v, P, i, o.hi.w, invmi);
-            wall_forces<MODEL, WCAP>(v, P, i, S.nneiw[lane], S.ncw[lane], o.hi, o.li, o.vi, o.wi, invmi, mt, F, err);
+            wall_forces<MODEL, WCAP, PER>(v, P, i, S.nneiw[lane], S.ncw[lane], o.hi, o.li, o.vi, o.wi, invmi, mt, F, err);
             o.vl = __ldg(&A.vell[i]);
             o.wl = __ldg(&A.rotl[i]);
             o.rh = __ldg(&v.refh[i]);
-            integrate_one(v, B, i, o, mt.invmoi, F, refresh, err);
+            integrate_one<PER>(v, B, i, o, mt.invmoi, F, refresh, err);
         }
         __syncwarp();
     }
@@ -1260,21 +1266,24 @@ __global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<
 namespace {
 // MINB: resident CTAs per SM a kernel's register allocation is sized for
 // (cooperative kernel 4, 5 or 6; one-pass kernel 2 or 3).
-template <int MODEL, int MINB>
+// PER: compiled for a periodic x; those kernels exist for the default
+// occupancy only (5 for the cooperative kernel, 2 for the one-pass kernel).
+template <int MODEL, int MINB, bool PER>
 void* direct_kernel_minb(int wall_cap) {
-    if (wall_cap <= 16) return (void*)k_step_mixed<MODEL, 16, MINB>;
-    if (wall_cap <= 32) return (void*)k_step_mixed<MODEL, 32, MINB>;
-    return (void*)k_step_mixed<MODEL, 64, MINB>;
+    if (wall_cap <= 16) return (void*)k_step_mixed<MODEL, 16, MINB, PER>;
+    if (wall_cap <= 32) return (void*)k_step_mixed<MODEL, 32, MINB, PER>;
+    return (void*)k_step_mixed<MODEL, 64, MINB, PER>;
 }
 template <int MODEL>
-void* direct_kernel(int wall_cap, int minb) {
-    return minb == 3 ? direct_kernel_minb<MODEL, 3>(wall_cap) : direct_kernel_minb<MODEL, 2>(wall_cap);
+void* direct_kernel(int wall_cap, int minb, bool per) {
+    if (per) return direct_kernel_minb<MODEL, 2, true>(wall_cap);
+    return minb == 3 ? direct_kernel_minb<MODEL, 3, false>(wall_cap) : direct_kernel_minb<MODEL, 2, false>(wall_cap);
 }
-template <int MODEL>
+template <int MODEL, bool PER>
 void* wtma_kernel(int wall_cap) {
-    void* fn = wall_cap <= 16   ? (void*)k_step_mixed_wtma<MODEL, 16>
-               : wall_cap <= 32 ? (void*)k_step_mixed_wtma<MODEL, 32>
-                                : (void*)k_step_mixed_wtma<MODEL, 64>;
+    void* fn = wall_cap <= 16   ? (void*)k_step_mixed_wtma<MODEL, 16, PER>
+               : wall_cap <= 32 ? (void*)k_step_mixed_wtma<MODEL, 32, PER>
+                                : (void*)k_step_mixed_wtma<MODEL, 64, PER>;
     static bool configured[3] = {false, false, false};
     const int slot = wall_cap <= 16 ? 0 : (wall_cap <= 32 ? 1 : 2);
     if (!configured[slot]) {
@@ -1283,11 +1292,11 @@ void* wtma_kernel(int wall_cap) {
     }
     return fn;
 }
-template <int MODEL, int MINB>
+template <int MODEL, int MINB, bool PER>
 void* coop_kernel_minb(int wall_cap) {
-    void* fn = wall_cap <= 16   ? (void*)k_step_mixed_coop<MODEL, 16, MINB>
-               : wall_cap <= 32 ? (void*)k_step_mixed_coop<MODEL, 32, MINB>
-                                : (void*)k_step_mixed_coop<MODEL, 64, MINB>;
+    void* fn = wall_cap <= 16   ? (void*)k_step_mixed_coop<MODEL, 16, MINB, PER>
+               : wall_cap <= 32 ? (void*)k_step_mixed_coop<MODEL, 32, MINB, PER>
+                                : (void*)k_step_mixed_coop<MODEL, 64, MINB, PER>;
     static bool configured[3] = {false, false, false};
     const int slot = wall_cap <= 16 ? 0 : (wall_cap <= 32 ? 1 : 2);
     if (!configured[slot]) {
@@ -1297,9 +1306,11 @@ void* coop_kernel_minb(int wall_cap) {
     return fn;
 }
 template <int MODEL>
-void* coop_kernel(int wall_cap, int minb) {
-    return minb == 4 ? coop_kernel_minb<MODEL, 4>(wall_cap)
-                     : (minb == 6 ? coop_kernel_minb<MODEL, 6>(wall_cap) : coop_kernel_minb<MODEL, 5>(wall_cap));
+void* coop_kernel(int wall_cap, int minb, bool per) {
+    if (per) return coop_kernel_minb<MODEL, 5, true>(wall_cap);
+    return minb == 4 ? coop_kernel_minb<MODEL, 4, false>(wall_cap)
+                     : (minb == 6 ? coop_kernel_minb<MODEL, 6, false>(wall_cap)
+                                  : coop_kernel_minb<MODEL, 5, false>(wall_cap));
 }
 // Kernel and occupancy: the engine's settings, else the environment
 // (GDEM_MIXED_KERNEL=staged|direct, GDEM_COOP_MINB, GDEM_MIXED_MINB), else the
@@ -1335,7 +1346,8 @@ StepLaunch step_launch(const View<Mixed>& v) {
     if (kind == 0) {
         static const int env_minb = env_int("GDEM_COOP_MINB", 5);
         const int minb = v.occupancy > 0 ? v.occupancy : env_minb;
-        void* fn = v.mat.model == 1 ? coop_kernel<1>(v.wall_cap, minb) : coop_kernel<0>(v.wall_cap, minb);
+        const bool per = v.per_x != 0;
+        void* fn = v.mat.model == 1 ? coop_kernel<1>(v.wall_cap, minb, per) : coop_kernel<0>(v.wall_cap, minb, per);
         const size_t smem = kCoopSmem;
         int per_sm = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kCoopWarps * 32, smem);
@@ -1346,7 +1358,8 @@ StepLaunch step_launch(const View<Mixed>& v) {
         return StepLaunch{fn, dim3(grid), dim3(kCoopWarps * 32), smem};
     }
     if (kind == 1) {
-        void* fn = v.mat.model == 1 ? wtma_kernel<1>(v.wall_cap) : wtma_kernel<0>(v.wall_cap);
+        void* fn = v.per_x ? (v.mat.model == 1 ? wtma_kernel<1, true>(v.wall_cap) : wtma_kernel<0, true>(v.wall_cap))
+                           : (v.mat.model == 1 ? wtma_kernel<1, false>(v.wall_cap) : wtma_kernel<0, false>(v.wall_cap));
         const int nsub = (v.n + 31) / 32;
         const int need = (nsub + kWarps - 1) / kWarps;
         const int grid = need < 2 * sm_count() ? need : 2 * sm_count();
@@ -1354,7 +1367,8 @@ StepLaunch step_launch(const View<Mixed>& v) {
     }
     static const int env_minb = env_int("GDEM_MIXED_MINB", 2);
     const int minb = v.occupancy > 0 ? v.occupancy : env_minb;
-    void* fn = v.mat.model == 1 ? direct_kernel<1>(v.wall_cap, minb) : direct_kernel<0>(v.wall_cap, minb);
+    const bool per = v.per_x != 0;
+    void* fn = v.mat.model == 1 ? direct_kernel<1>(v.wall_cap, minb, per) : direct_kernel<0>(v.wall_cap, minb, per);
     return StepLaunch{fn, dim3(ntiles), dim3(kBlock), 0};
 }
 
