@@ -36,7 +36,11 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "particle-steps/s at 1M spheres, FP32-mixed vs FP64 plain on 1 GB300 (err≤1e-4·r_min)"
-TRAFFIC_POURED_BED_1M = 809_291_520.0   # bytes per step-kernel launch, ncu on the default workload
+TRAFFIC_POURED_BED_1M = 808_314_880.0   # bytes per step-kernel launch, ncu on the default workload
+# bytes per sphere of one step-kernel launch on the periodic channel, from an
+# ncu capture of the 1M-sphere channel (the 10M one is too large to capture);
+# the launch's traffic scales with the spheres it steps
+TRAFFIC_CHANNEL_PER_SPHERE = 274_364_416.0 / 1_000_000
 UNIT = "particle-steps/s"
 METRIC_CHANNEL = "particle-steps/s at 10M spheres in a channel periodic in x, FP32-mixed on 1 GB300"
 
@@ -225,6 +229,16 @@ def run_engine(args):
     k_ms = E.profile_step(args.profile_iters)
     _nvtx()
     stk = E.stats()
+    # one forced list rebuild (keys, sort, reorder, cells, Verlet and wall
+    # lists), CUDA events on the engine stream around the call
+    _nvtx("rebuild")
+    rb0, rb1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    rb0.record(stream)
+    E.rebuild()
+    rb1.record(stream)
+    rb1.synchronize()
+    _nvtx()
+    rebuild_ms = rb0.elapsed_time(rb1)
     mixed = args.precision == "mixed"
     bytes_launch = algorithmic_bytes(stk, stk["n_active"], s=4 if mixed else 8, s_h=8)
     peak, peak_kind = _peaks()
@@ -234,6 +248,9 @@ def run_engine(args):
         # dram__bytes_read.sum + dram__bytes_write.sum of one launch on this
         # workload (profiles/k_step_mixed_coop_poured_bed_1M.txt)
         traffic = TRAFFIC_POURED_BED_1M
+    if traffic is None and mixed and args.workload == "channel" and args.model == "hertz_mindlin":
+        # (profiles/k_step_mixed_coop_channel_1M.txt), scaled to this launch's spheres
+        traffic = TRAFFIC_CHANNEL_PER_SPHERE * stk["n_active"]
     reb = int(st1["rebuilds"] - st0["rebuilds"])
     E.close()
     extra = {}
@@ -269,7 +286,8 @@ def run_engine(args):
                    "model": args.model, "l2": "inputs larger than L2 (state + lists > 129 MB per step)",
                    "parallelism": "replicas" if ws > 1 else "single GPU",
                    "lbvh": "built once (static mesh)" if args.bvh_once else "rebuilt every step",
-                   "rebuilds_in_timed_region": reb, "setup_s": round(setup_s, 2), "pour_s": round(pour_s, 1),
+                   "rebuilds_in_timed_region": reb, "rebuild_ms": round(rebuild_ms, 3),
+                   "setup_s": round(setup_s, 2), "pour_s": round(pour_s, 1),
                    "contacts_per_sphere": round(stk["n_contacts"] / max(stk["n_active"], 1), 3),
                    "wall_contacts_per_sphere": round(stk["n_wall_contacts"] / max(stk["n_active"], 1), 3),
                    **extra},
