@@ -104,10 +104,15 @@ class Clocks:
 
 def algorithmic_bytes(st, n_active, s=8, s_h=8):
     """Force-kernel bytes per launch: N(S_read+S_write) + 4(2N + sum n_nei +
-    sum n_w) + (sum n_c + sum n_wc)(6 s_h + 8), S_read = 24 + 8s, S_write = 24 + 6s."""
+    sum n_w) + (sum n_c + sum n_wc)(6 s_h + 8), S_read = 24 + 8s, S_write = 24 + 6s.
+    With inner rows the step reads those instead of the list rows (sum n_inner
+    for sum n_nei, sum n_inner_wall for sum n_w)."""
     s_read = 24 + 6 * s + 2 * s
     s_write = 24 + 6 * s
-    return (n_active * (s_read + s_write) + 4 * (2 * n_active + st["n_nei"] + st["n_wall"])
+    inner = st.get("n_inner", 0) > 0
+    rows = st["n_inner"] if inner else st["n_nei"]
+    wrows = st["n_inner_wall"] if inner else st["n_wall"]
+    return (n_active * (s_read + s_write) + 4 * (2 * n_active + rows + wrows)
             + (st["n_contacts"] + st["n_wall_contacts"]) * (6 * s_h + 8))
 
 
@@ -302,7 +307,7 @@ def run_engine(args):
                      "peak_kind": f"{peak_kind} hbm_gbs",
                      "kernel": f"k_step<{'Mixed' if mixed else 'FP64'},{args.model}>", "kernel_ms": k_ms,
                      "algorithmic_bytes": bytes_launch,
-                     "counts": {k: stk[k] for k in ("n_active", "n_nei", "n_wall", "n_contacts",
+                     "counts": {k: stk[k] for k in ("n_active", "n_nei", "n_inner", "n_wall", "n_inner_wall", "n_contacts",
                                                     "n_wall_contacts")}},
         "e2e": e2e,
         "cpu_baseline": cpu_baseline(args, sc) if (rank == 0 and ws == 1 and not args.no_cpu) else None,

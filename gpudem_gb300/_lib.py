@@ -45,7 +45,7 @@ class Desc(C.Structure):
         ("youngs_modulus", C.c_double), ("poisson_ratio", C.c_double),
         ("restitution", C.c_double), ("rolling_friction", C.c_double),
         ("bvh_every_step", C.c_int), ("mixed_kernel", C.c_int), ("occupancy", C.c_int),
-        ("periodic_x", C.c_int),
+        ("periodic_x", C.c_int), ("inner_skin", C.c_double),
     ]
 
 
@@ -70,7 +70,8 @@ class Stats(C.Structure):
         ("n_wall_contacts", C.c_longlong), ("kinetic_energy", C.c_double),
         ("coordination", C.c_double), ("packing_fraction", C.c_double),
         ("max_overlap", C.c_double), ("error_word", C.c_uint), ("max_nei", C.c_int),
-        ("max_wall", C.c_int),
+        ("max_wall", C.c_int), ("n_inner", C.c_longlong), ("inner_builds", C.c_longlong),
+        ("n_inner_wall", C.c_longlong),
     ]
 
 

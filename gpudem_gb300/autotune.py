@@ -3,8 +3,9 @@
 Picks, for one scene, the mixed-precision step kernel and the occupancy it is
 compiled for (the block configuration), the Verlet skin (which sets the list
 cutoff and, through the refresh threshold skin/2, the rebuild cadence), the
-cell size, and the number of steps per CUDA-graph launch, by timing short runs
-of each candidate on the GPU.  The skin, cell size and graph length leave the
+cell size, the inner skin (the rows the step scans and their rebuild cadence),
+and the number of steps per CUDA-graph launch, by timing short runs of each
+candidate on the GPU.  The skin, cell size and graph length leave the
 trajectory unchanged: the lists only decide which pairs are tested, the
 contact set is the same while they are valid, and forces are summed in
 partner-pId order whatever the storage order.  The kernel variants compute
@@ -25,6 +26,7 @@ import numpy as np
 # warp-staged, one thread per particle at 2/3 CTAs per SM
 KERNELS = [(1, 4), (1, 5), (1, 6), (2, 0), (3, 2), (3, 3)]
 SKIN_FACTORS = [0.5, 1.0, 1.5]          # x r_max
+INNER_FACTORS = [0.05, 0.1, 0.2]        # x r_max (at most the skin)
 GRAPH_STEPS = [4, 8, 16]
 
 
@@ -59,6 +61,8 @@ def candidate_stages(scene, precision: str):
         stages.append([dict(mixed_kernel=k, occupancy=o) for k, o in KERNELS])
     skins = [f * rmax for f in SKIN_FACTORS]
     stages.append([dict(skin=s, cell_size=max(4.0 * rmax, 2.0 * rmax + s)) for s in skins])
+    if precision == "mixed":
+        stages.append([dict(inner_skin=f * rmax) for f in INNER_FACTORS])
     stages.append([dict(steps_per_graph=k) for k in GRAPH_STEPS])
     return stages
 

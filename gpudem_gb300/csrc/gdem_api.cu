@@ -188,6 +188,13 @@ struct Impl : EngineBase {
         A.add(&v.nneiw, n);
         if (T::mixed) {
             A.add(&v.refh, n);
+            if (d.inner_skin >= 0.) {
+                A.add(&v.inn, (size_t)n * v.nei_cap);
+                A.add(&v.ninn, n);
+                A.add(&v.innw, (size_t)n * v.wall_cap);
+                A.add(&v.ninnw, n);
+                A.add(&v.refi, n);
+            }
         } else {
             A.add(&v.ref, n);
             A.add(&v.posf, n);
@@ -299,16 +306,35 @@ struct Impl : EngineBase {
         }
     }
 
+    // The view the step kernels get: with inner rows, they scan those in
+    // place of the list rows.
+    View<T> sv() const {
+        View<T> s = v;
+        if (v.inner_on) {
+            s.nei = v.inn;
+            s.nnei = v.ninn;
+            s.neiw = v.innw;
+            s.nneiw = v.ninnw;
+        }
+        return s;
+    }
+
     int build_graph(int steps, cudaGraphExec_t* out) {
         cudaGraph_t g;
         CKE(cudaGraphCreate(&g, 0));
         cudaGraphNode_t prev = nullptr;
-        const StepLaunch L = step_launch(v);
+        View<T> vs = sv();
+        const StepLaunch L = step_launch(vs);
         for (int k = 0; k < steps; k++) {
-            cudaGraphConditionalHandle hnd;
+            // every handle must belong to a conditional node: the inner-rows
+            // handle exists only with inner rows (else the kernel gets hnd twice
+            // and leaves the second alone)
+            cudaGraphConditionalHandle hnd, hin;
             CKE(cudaGraphConditionalHandleCreate(&hnd, g, 0, cudaGraphCondAssignDefault));
-            int use_cond = 1;
-            void* args[3] = {(void*)&v, (void*)&hnd, (void*)&use_cond};
+            hin = hnd;
+            if (v.inner_on) CKE(cudaGraphConditionalHandleCreate(&hin, g, 0, cudaGraphCondAssignDefault));
+            int use_cond = v.inner_on ? 3 : 1;
+            void* args[4] = {(void*)&vs, (void*)&hnd, (void*)&hin, (void*)&use_cond};
             cudaKernelNodeParams kp = {};
             kp.func = L.fn;
             kp.gridDim = L.grid;
@@ -341,6 +367,23 @@ struct Impl : EngineBase {
             cudaGraph_t captured;
             CKE(cudaStreamEndCapture(st, &captured));
             prev = cn;
+            if (v.inner_on) {
+                // new inner rows when some particle moved half the inner skin
+                // (after a list rebuild, its own body already made them)
+                cudaGraphNodeParams ip = {};
+                ip.type = cudaGraphNodeTypeConditional;
+                ip.conditional.handle = hin;
+                ip.conditional.type = cudaGraphCondTypeIf;
+                ip.conditional.size = 1;
+                cudaGraphNode_t in;
+                CKE(cudaGraphAddNode(&in, g, &prev, nullptr, 1, &ip));
+                CKE(cudaStreamBeginCaptureToGraph(st, ip.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                                  cudaStreamCaptureModeThreadLocal));
+                launch_inner(v, st);
+                cudaGraph_t cap2;
+                CKE(cudaStreamEndCapture(st, &cap2));
+                prev = in;
+            }
         }
         CKE(cudaGraphInstantiate(out, g, 0));
         cudaGraphDestroy(g);
@@ -425,6 +468,16 @@ struct Impl : EngineBase {
         v.skin = skin;
         v.thresh_sq = thresh * thresh;
         v.thresh_sqf = (float)v.thresh_sq;
+        // inner rows (mixed mode): a tenth of r_max by default, never more than the skin
+        v.inner_on = 0;
+        if (T::mixed && d.inner_skin >= 0.) {
+            double si = d.inner_skin > 0. ? d.inner_skin : 0.1 * rmax;
+            if (si > skin) si = skin;
+            v.inner_on = 1;
+            v.inner_skin = si;
+            v.inner_skinf = (float)si;
+            v.inner_thresh_sqf = (float)(0.25 * si * si);
+        }
         v.invdx = v.invdy = v.invdz = 1. / cell;
         v.sizex = (int)ceil((v.maxx - v.minx) / cell) + 2;
         if (v.per_x) {
@@ -533,7 +586,7 @@ struct Impl : EngineBase {
         if (!use_graphs) {
             // plain launches: step kernel, then the device-gated rebuild
             for (int q = 0; q < nsteps; q++) {
-                launch_step(v, st, 0, 0);
+                launch_step(sv(), st, 0, 0);
                 if (d.bvh_every_step && mesh) launch_bvh_rebuild(*mesh, st);
                 launch_rebuild(v, st, /*force=*/0);
             }
@@ -753,7 +806,7 @@ struct Impl : EngineBase {
         Ctl c;
         CKE(cudaMemcpy(&c, v.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
         double acc[7] = {0, 0, 0, 0, 0, 0, 0};
-        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300}, mo = 0.;
+        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300}, mo = 0., ninn_sum = 0., ninnw_sum = 0.;
         for (int b = 0; b < stats_nblk; b++) {
             const double* q = &part[(size_t)16 * b];
             for (int k = 0; k < 7; k++) acc[k] += q[k];
@@ -762,6 +815,8 @@ struct Impl : EngineBase {
                 hi[k] = std::max(hi[k], q[10 + k]);
             }
             mo = std::max(mo, q[13]);
+            ninn_sum += q[14];
+            ninnw_sum += q[15];
         }
         memset(s, 0, sizeof(*s));
         s->steps = (long long)c.steps;
@@ -779,6 +834,9 @@ struct Impl : EngineBase {
         s->error_word = c.error;
         s->max_nei = c.max_nei;
         s->max_wall = c.max_wall;
+        s->n_inner = (long long)ninn_sum;
+        s->inner_builds = (long long)c.inner_builds;
+        s->n_inner_wall = (long long)ninnw_sum;
         return GDEM_OK;
     }
 
@@ -818,7 +876,7 @@ struct Impl : EngineBase {
         for (auto& e : ev) CKE(cudaEventCreate(&e));
         for (int q = 0; q < groups; q++) {
             CKE(cudaEventRecord(ev[2 * q], st));
-            for (int b = 0; b < kProfileBurst; b++) launch_step(v, st, 0, 0);
+            for (int b = 0; b < kProfileBurst; b++) launch_step(sv(), st, 0, 0);
             CKE(cudaEventRecord(ev[2 * q + 1], st));
             launch_rebuild(v, st, /*force=*/0);
         }

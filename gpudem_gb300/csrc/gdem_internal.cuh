@@ -91,6 +91,9 @@ struct Ctl {
     int max_nei, max_wall;
     int lists_valid;
     unsigned work;            // next sub-tile of the persistent step kernel (0 between steps)
+    unsigned irefresh;        // mixed mode: the inner rows are to be rebuilt
+    unsigned pad;
+    unsigned long long inner_builds;
 };
 
 template <class T>
@@ -156,6 +159,17 @@ struct View {
     float4* refh;                    // mixed mode: {hi.xyz, -} at the last rebuild
     float4* posf;                    // FP64 mode: FP32 positions for the list prefilter
     int nei_cap, wall_cap, hist_cap, histw_cap;
+    // mixed mode, inner rows: the partners of each list row within
+    // r_i + r_j + inner skin, in row order, and the high-part positions they
+    // were taken at; the step kernels scan these instead of the list rows
+    int* inn;
+    int* ninn;
+    int* innw;                       // ... and the wall-row triangles within r + inner skin
+    int* ninnw;
+    float4* refi;
+    int inner_on;
+    double inner_skin;
+    float inner_skinf, inner_thresh_sqf;
     // per-step force/torque output
     double *fx, *fy, *fz, *tx, *ty, *tz;
     double* ftmp;                    // [6 * n] scratch for reordering the force outputs
@@ -436,6 +450,9 @@ int rs_blocks_for(int n);
 void launch_dist_triangle(const TriRec* tri, const double* pos, const double* r, const int* t, int m,
                           double* out4, int* hit, cudaStream_t st);
 void launch_trif(const TriRec* tri, TriRecF* out, TriLoF* lo, int ntri, cudaStream_t st);
+// inner rows (mixed mode with inner rows; gated on ctl->irefresh)
+template <class T>
+void launch_inner(const View<T>& v, cudaStream_t st);
 
 // float pair split of an FP64 value: x == hi + lo to within 2^-48 |x|
 __device__ __forceinline__ void split2(double x, float& hi, float& lo) {

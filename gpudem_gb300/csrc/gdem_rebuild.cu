@@ -559,11 +559,80 @@ __global__ void __launch_bounds__(kBlock) k_wall_lists(View<T> v, int gated) {
             ctl->refresh = 0u;
             ctl->rebuilds += 1ull;
             ctl->lists_valid = 1;
+            ctl->irefresh = 1u;  // new list rows (and storage order): new inner rows
+        }
+    }
+}
+
+// ===================================================================== inner rows
+// Mixed mode: the partners of each list row within r_i + r_j + inner skin,
+// in row order (so in partner-pId order), the wall-row triangles within
+// r_i + inner skin (FP64 closest feature, in row order), and the high-part
+// positions they were taken at.  The test runs on the high parts with the list prefilter's
+// error bound added to the cutoff, so it keeps every pair that is within the
+// cutoff in exact arithmetic.  A pair left out is more than the inner skin
+// apart, and it cannot touch before some particle has moved half the inner
+// skin, when the step asks for new rows (ctl->irefresh); every list rebuild
+// asks too.  Gated on that request in every launch mode.
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_inner(View<T> v) {
+    Ctl* ctl = v.ctl;
+    if (ctl->irefresh == 0u) return;
+    const int n = v.n;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if constexpr (T::mixed) {
+        if (i < n) {
+            const SBank<T> S = v.S[ctl->s];
+            const float4 hi = S.posh[i];
+            int m = 0;
+            if (hi.w > 0.f) {
+                const int nn = v.nnei[i];
+                const float cut = v.inner_skinf + v.nb_delta;
+                for (int k = 0; k < nn; k++) {
+                    const int j = v.nei[(size_t)k * n + i];
+                    const float4 hj = S.posh[j];
+                    if (!(hj.w > 0.f)) continue;  // inactive for good
+                    const float dx = image_dxf(v, hi.x - hj.x), dy = hi.y - hj.y, dz = hi.z - hj.z;
+                    const float R = hi.w + hj.w + cut;
+                    if (dx * dx + dy * dy + dz * dz < R * R * 1.0000039f) {
+                        if (m < v.nei_cap) v.inn[(size_t)m * n + i] = j;
+                        m++;
+                    }
+                }
+            }
+            v.ninn[i] = m < v.nei_cap ? m : v.nei_cap;
+            int mw = 0;
+            if (hi.w > 0.f && v.ntri > 0) {
+                const double4_32a p = load_pos(S, i);
+                const double R = p.w + v.inner_skin;
+                const int nw = v.nneiw[i];
+                for (int k = 0; k < nw; k++) {
+                    const int t = v.neiw[(size_t)k * n + i];
+                    const Feature f = closest_feature(image_x_near(v, p.x, v.tri[t].v0[0]), p.y, p.z, R * R, v.tri[t]);
+                    if (f.dist < R) v.innw[(size_t)mw++ * n + i] = t;
+                }
+            }
+            v.ninnw[i] = mw;
+            v.refi[i] = make_float4(hi.x, hi.y, hi.z, 0.f);
+        }
+    }
+    if (last_block(&ctl->done[3])) {
+        if (threadIdx.x == 0) {
+            ctl->done[3] = 0;
+            ctl->irefresh = 0u;
+            ctl->inner_builds += 1ull;
         }
     }
 }
 
 static inline int grid_for(int n) { return (n + kBlock - 1) / kBlock; }
+
+template <class T>
+void launch_inner(const View<T>& v, cudaStream_t st) {
+    if (T::mixed && v.inner_on) k_inner<T><<<grid_for(v.n), kBlock, 0, st>>>(v);
+}
+template void launch_inner<FP64>(const View<FP64>&, cudaStream_t);
+template void launch_inner<Mixed>(const View<Mixed>&, cudaStream_t);
 
 template <class T>
 void launch_rebuild(const View<T>& v, cudaStream_t st, int force) {
@@ -597,6 +666,7 @@ void launch_rebuild(const View<T>& v, cudaStream_t st, int force) {
         k_wall_lists<T, 32><<<g, kBlock, 0, st>>>(v, gated);
     else
         k_wall_lists<T, 64><<<g, kBlock, 0, st>>>(v, gated);
+    launch_inner(v, st);
 }
 
 template void launch_rebuild<FP64>(const View<FP64>&, cudaStream_t, int);

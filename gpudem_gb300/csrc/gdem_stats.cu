@@ -12,7 +12,7 @@
 namespace gdem {
 
 constexpr int kStatBlocks = 1024;
-constexpr int kNStat = 14;
+constexpr int kNStat = 16;
 
 int stats_blocks(int n) {
     const int g = (n + kBlock - 1) / kBlock;
@@ -51,6 +51,10 @@ __global__ void __launch_bounds__(kBlock) k_stats(View<T> v, double* partials) {
         acc[10] = fmax(acc[10], p.x + r);
         acc[11] = fmax(acc[11], p.y + r);
         acc[12] = fmax(acc[12], p.z + r);
+        if (v.inner_on) {
+            acc[14] += v.ninn[i];
+            acc[15] += v.ninnw[i];
+        }
         const int nn = v.nnei[i];
         for (int k = 0; k < nn; k++) {
             const int j = v.nei[(size_t)k * n + i];
@@ -70,6 +74,8 @@ __global__ void __launch_bounds__(kBlock) k_stats(View<T> v, double* partials) {
             for (int k = 0; k < 7; k++) sm[k][threadIdx.x] += sm[k][threadIdx.x + o];
             for (int k = 7; k < 10; k++) sm[k][threadIdx.x] = fmin(sm[k][threadIdx.x], sm[k][threadIdx.x + o]);
             for (int k = 10; k < 14; k++) sm[k][threadIdx.x] = fmax(sm[k][threadIdx.x], sm[k][threadIdx.x + o]);
+            sm[14][threadIdx.x] += sm[14][threadIdx.x + o];
+            sm[15][threadIdx.x] += sm[15][threadIdx.x + o];
         }
         __syncthreads();
     }

@@ -129,6 +129,7 @@ __device__ __forceinline__ int find_slot(const int* hid, int n, int i, int& nc, 
 
 template <class T, int MODEL, int WCAP>
 __global__ void __launch_bounds__(kBlock) k_step(View<T> v, cudaGraphConditionalHandle cond,
+                                                 cudaGraphConditionalHandle /*inner rows: mixed mode only*/,
                                                  int use_cond) {
     using R = typename T::real;
     using V4 = typename T::v4;
@@ -491,7 +492,8 @@ void launch_step_any(const View<T>& v, cudaStream_t st, cudaGraphConditionalHand
     const int g = (v.n + kBlock - 1) / kBlock;
     void* fn = step_kernel_any<T>(v);
     View<T> vv = v;
-    void* args[3] = {(void*)&vv, (void*)&cond, (void*)&use_cond};
+    cudaGraphConditionalHandle ci = cond;
+    void* args[4] = {(void*)&vv, (void*)&cond, (void*)&ci, (void*)&use_cond};
     cudaLaunchKernel(fn, dim3(g), dim3(kBlock), args, 0, st);
 }
 

@@ -319,11 +319,20 @@ __device__ __forceinline__ float wall_overlap(float3 ph, float3 pl, float rh, fl
 
 }  // namespace
 
-// End of a step kernel: refresh vote, error bits, and in the last CTA the
-// bank flip, the step count and the graph's rebuild condition.
-__device__ __forceinline__ void step_epilogue(Ctl* ctl, int s, bool refresh, unsigned err,
-                                              cudaGraphConditionalHandle cond, int use_cond) {
-    if (__any_sync(0xffffffffu, refresh) && (threadIdx.x & 31) == 0) atomicOr(&ctl->refresh, 1u);
+// Refresh votes of a thread: the list rows (bit 0) and the inner rows (bit 1).
+constexpr unsigned kVoteLists = 1u, kVoteInner = 2u;
+
+// End of a step kernel: refresh votes, error bits, and in the last CTA the
+// bank flip, the step count and the graph's rebuild conditions (list rebuild;
+// inner rows, when use_cond has bit 1).
+__device__ __forceinline__ void step_epilogue(Ctl* ctl, int s, unsigned votes, unsigned err,
+                                              cudaGraphConditionalHandle cond, cudaGraphConditionalHandle ci,
+                                              int use_cond) {
+    const unsigned wv = __reduce_or_sync(0xffffffffu, votes);
+    if ((threadIdx.x & 31) == 0) {
+        if (wv & kVoteLists) atomicOr(&ctl->refresh, 1u);
+        if (wv & kVoteInner) atomicOr(&ctl->irefresh, 1u);
+    }
     if (err) atomicOr(&ctl->error, err);
     if (last_block(&ctl->done[0])) {
         if (threadIdx.x == 0) {
@@ -333,6 +342,7 @@ __device__ __forceinline__ void step_epilogue(Ctl* ctl, int s, bool refresh, uns
             ctl->steps += 1ull;
             const unsigned r = atomicAdd(&ctl->refresh, 0u);
             if (use_cond) cudaGraphSetConditional(cond, r ? 1u : 0u);
+            if (use_cond & 2) cudaGraphSetConditional(ci, atomicAdd(&ctl->irefresh, 0u) ? 1u : 0u);
         }
     }
 }
@@ -622,7 +632,7 @@ __device__ __forceinline__ void freeze_one(const View<Mixed>& v, const SBank<Mix
 // refresh and out-of-box tests; the new state into bank s^1.
 template <bool PER>
 __device__ __forceinline__ void integrate_one(const View<Mixed>& v, const SBank<Mixed>& B, int i, const Own& o,
-                                              float invmoi, const Force6& F, bool& refresh, unsigned& err) {
+                                              float invmoi, const Force6& F, unsigned& votes, unsigned& err) {
     using R = float;
     const PerX per = per_of<PER>(v);
     const R dt = v.dtf;
@@ -659,15 +669,23 @@ __device__ __forceinline__ void integrate_one(const View<Mixed>& v, const SBank<
     pair_add(nwz, wl.z, F.mz * invmoi * dt);
     B.vell[i] = vl;
     B.rotl[i] = wl;
-    // refresh test against the position of the last rebuild, on the high
-    // parts: it only decides when the lists are rebuilt, and the threshold
-    // leaves a margin of skin/2 to the list cutoff.  The flag is sticky: the
-    // persistent kernels integrate many particles per thread.
+    // refresh tests against the positions of the last list rebuild and of the
+    // last inner rows, on the high parts: they only decide when rows are
+    // rebuilt, and each threshold leaves a margin of half its skin to its
+    // cutoff.  The votes are sticky: the persistent kernels integrate many
+    // particles per thread.
     {
         R ex = nh.x - o.rh.x;
         if (per.on) ex = ex > per.half ? ex - per.Lh : (ex < -per.half ? ex + per.Lh : ex);
         const R ey = nh.y - o.rh.y, ez = nh.z - o.rh.z;
-        if (ex * ex + ey * ey + ez * ez > v.thresh_sqf) refresh = true;
+        if (ex * ex + ey * ey + ez * ez > v.thresh_sqf) votes |= kVoteLists;
+    }
+    if (v.inner_on) {
+        const float4 rf = v.refi[i];
+        R ex = nh.x - rf.x;
+        if (per.on) ex = ex > per.half ? ex - per.Lh : (ex < -per.half ? ex + per.Lh : ex);
+        const R ey = nh.y - rf.y, ez = nh.z - rf.z;
+        if (ex * ex + ey * ey + ez * ez > v.inner_thresh_sqf) votes |= kVoteInner;
     }
     // out of bounds (the box rounded outwards to FP32; not in a periodic x)
     R status = 1.f;
@@ -694,7 +712,7 @@ __device__ __forceinline__ void integrate_one(const View<Mixed>& v, const SBank<
 // contacts, integration.  Writes bank s^1 and the history.
 template <int MODEL, int WCAP, bool PER>
 __device__ __forceinline__ void step_one(const View<Mixed>& v, const SBank<Mixed>& A, const SBank<Mixed>& B,
-                                         const PBank<Mixed>& P, int i, const Own& o, bool& refresh, unsigned& err,
+                                         const PBank<Mixed>& P, int i, const Own& o, unsigned& votes, unsigned& err,
                                          const int* nei_s = nullptr, int nei_s_rows = 0) {
     using T = Mixed;
     using R = float;
@@ -768,12 +786,12 @@ __device__ __forceinline__ void step_one(const View<Mixed>& v, const SBank<Mixed
     }
     P.nc[i] = surviving(touched, nc);
     wall_forces<MODEL, WCAP, PER>(v, P, i, o.nw, o.ncw, hi, li, o.vi, o.wi, invmi, mt, F, err);
-    integrate_one<PER>(v, B, i, o, mt.invmoi, F, refresh, err);
+    integrate_one<PER>(v, B, i, o, mt.invmoi, F, votes, err);
 }
 
 // One thread per particle, state loaded straight from HBM.
 template <int MODEL, int WCAP, int MINB, bool PER>
-__global__ void __launch_bounds__(kBlock, MINB) k_step_mixed(View<Mixed> v, cudaGraphConditionalHandle cond,
+__global__ void __launch_bounds__(kBlock, MINB) k_step_mixed(View<Mixed> v, cudaGraphConditionalHandle cond, cudaGraphConditionalHandle cond_inner,
                                                             int use_cond) {
     Ctl* ctl = v.ctl;
     const int s = ctl->s, p = ctl->p;
@@ -781,7 +799,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_step_mixed(View<Mixed> v, cuda
     const SBank<Mixed> A = v.S[s];
     const SBank<Mixed> B = v.S[s ^ 1];
     const PBank<Mixed> P = v.P[p];
-    bool refresh = false;
+    unsigned votes = 0u;
     unsigned err = 0u;
     if (i < v.n) {
         Own o;
@@ -796,9 +814,9 @@ __global__ void __launch_bounds__(kBlock, MINB) k_step_mixed(View<Mixed> v, cuda
         o.nw = __ldg(&v.nneiw[i]);
         o.nc = P.nc[i];
         o.ncw = P.ncw[i];
-        step_one<MODEL, WCAP, PER>(v, A, B, P, i, o, refresh, err);
+        step_one<MODEL, WCAP, PER>(v, A, B, P, i, o, votes, err);
     }
-    step_epilogue(ctl, s, refresh, err, cond, use_cond);
+    step_epilogue(ctl, s, votes, err, cond, cond_inner, use_cond);
 }
 
 // ---------------------------------------------------------------- bulk copies
@@ -885,7 +903,7 @@ __device__ __forceinline__ void issue_sub(const View<Mixed>& v, const SBank<Mixe
 }
 
 template <int MODEL, int WCAP, bool PER>
-__global__ void __launch_bounds__(kBlock, 2) k_step_mixed_wtma(View<Mixed> v, cudaGraphConditionalHandle cond,
+__global__ void __launch_bounds__(kBlock, 2) k_step_mixed_wtma(View<Mixed> v, cudaGraphConditionalHandle cond, cudaGraphConditionalHandle cond_inner,
                                                               int use_cond) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -899,7 +917,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_step_mixed_wtma(View<Mixed> v, cu
     const int nsub = (v.n + 31) / 32;
     const int stride = gridDim.x * kWarps;
     const int nei_rows = (v.n % 4 == 0) ? min(kNeiStageRows, v.nei_cap) : 0;
-    bool refresh = false;
+    unsigned votes = 0u;
     unsigned err = 0u;
     if (lane == 0) {
         mbar_init(&full[warp][0], 1);
@@ -941,7 +959,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_step_mixed_wtma(View<Mixed> v, cu
             o.nw = S.nneiw[lane];
             o.nc = S.nc[lane];
             o.ncw = S.ncw[lane];
-            step_one<MODEL, WCAP, PER>(v, A, B, P, i, o, refresh, err, &S.nei[0][lane], nei_rows);
+            step_one<MODEL, WCAP, PER>(v, A, B, P, i, o, votes, err, &S.nei[0][lane], nei_rows);
         }
         __syncwarp();
     }
@@ -954,7 +972,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_step_mixed_wtma(View<Mixed> v, cu
         }
         __syncwarp();
     }
-    step_epilogue(ctl, s, refresh, err, cond, use_cond);
+    step_epilogue(ctl, s, votes, err, cond, cond_inner, use_cond);
 }
 
 // ---------------------------------------------------------------- warp-cooperative
@@ -1043,7 +1061,7 @@ __device__ __forceinline__ int find_slot_staged(int* hid_s, int rows, int* hid, 
 }
 
 template <int MODEL, int WCAP, int MINB, bool PER>
-__global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<Mixed> v, cudaGraphConditionalHandle cond,
+__global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<Mixed> v, cudaGraphConditionalHandle cond, cudaGraphConditionalHandle cond_inner,
                                                                     int use_cond) {
     using R = float;
     constexpr int Q = kCoopQ;
@@ -1067,7 +1085,7 @@ __global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<
     const int nei_rows = (n % 4 == 0) ? min(kNeiStageRows, v.nei_cap) : 0;
     const int hid_rows = (n % 4 == 0) ? min(kHidStageRows, v.hist_cap) : 0;
     const PerX per = per_of<PER>(v);
-    bool refresh = false;
+    unsigned votes = 0u;
     unsigned err = 0u;
     if (lane == 0) {
         mbar_init(&full[warp][0], 1);
@@ -1247,7 +1265,7 @@ __global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<
             o.vl = __ldg(&A.vell[i]);
             o.wl = __ldg(&A.rotl[i]);
             o.rh = __ldg(&v.refh[i]);
-            integrate_one<PER>(v, B, i, o, mt.invmoi, F, refresh, err);
+            integrate_one<PER>(v, B, i, o, mt.invmoi, F, votes, err);
         }
         __syncwarp();
     }
@@ -1260,7 +1278,7 @@ __global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<
         }
         __syncwarp();
     }
-    step_epilogue(ctl, s, refresh, err, cond, use_cond);
+    step_epilogue(ctl, s, votes, err, cond, cond_inner, use_cond);
 }
 
 namespace {
@@ -1375,7 +1393,8 @@ StepLaunch step_launch(const View<Mixed>& v) {
 void launch_step(const View<Mixed>& v, cudaStream_t st, cudaGraphConditionalHandle cond, int use_cond) {
     const StepLaunch L = step_launch(v);
     View<Mixed> vv = v;
-    void* args[3] = {(void*)&vv, (void*)&cond, (void*)&use_cond};
+    cudaGraphConditionalHandle ci = cond;
+    void* args[4] = {(void*)&vv, (void*)&cond, (void*)&ci, (void*)&use_cond};
     cudaLaunchKernel(L.fn, L.grid, L.block, args, L.smem, st);
 }
 

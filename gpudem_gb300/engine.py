@@ -43,12 +43,14 @@ def box_limits(tris: np.ndarray, inlet_lo, inlet_hi):
 
 class Engine:
     """One scene on the GPU.  ``precision`` is "fp64" (bit-compatible with the
-    reference CPU path) or "mixed"; ``model`` is "linear" or "hertz_mindlin"."""
+    reference CPU path) or "mixed"; ``model`` is "linear" or "hertz_mindlin".
+    ``inner_skin`` (mixed): skin of the inner rows the step scans (0: 0.1 r_max,
+    negative: none, the step scans the list rows); results do not depend on it."""
 
     def __init__(self, scene: Scene, precision="fp64", model="linear", reorder=True,
                  store_forces=False, nei_capacity=64, wall_capacity=32, hist_capacity=32,
                  hist_wall_capacity=16, steps_per_graph=8, cell_size=-1.0, skin=None,
-                 refresh=None, box=None, bvh_every_step=False, mixed_kernel=0, occupancy=0):
+                 refresh=None, box=None, bvh_every_step=False, mixed_kernel=0, occupancy=0, inner_skin=0.0):
         self.L = _lib.load()
         self.scene = scene
         self.n = scene.n
@@ -85,6 +87,7 @@ class Engine:
         d.mixed_kernel = int(mixed_kernel)
         d.occupancy = int(occupancy)
         d.periodic_x = 1 if scene.periodic_x else 0
+        d.inner_skin = float(inner_skin)
         self.desc = d
         h = C.c_void_p()
         _lib.check(self.L.gdem_create(C.byref(d), C.byref(h)), None, "gdem_create")

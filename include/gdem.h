@@ -91,6 +91,13 @@ typedef struct gdem_desc {
      * are L/floor(L/cell_size) wide in x (at least 3 of them).  No reference
      * counterpart (the reference's box only deactivates what leaves it). */
     int periodic_x;
+    /* mixed precision: skin of the inner rows the step kernel scans, the partners
+     * of each list row within r_i + r_j + inner_skin, rebuilt from the list rows
+     * when a particle has moved half of it (and after every list rebuild).  The
+     * contacts and their order are those of the list rows, so results do not
+     * change.  0: 0.1 * r_max (at most the skin); < 0: off, the step scans the
+     * list rows. */
+    double inner_skin;
 } gdem_desc;
 
 /* Particle arrays in the reference layout (memberList/ParticleSystemMember_common.def).
@@ -137,6 +144,9 @@ typedef struct gdem_stats {
     double max_overlap;         /* max over contacts of overlap / (2 r_i) */
     unsigned int error_word;    /* GDEM_EW_* bits */
     int max_nei, max_wall;      /* longest lists seen at the last rebuild */
+    long long n_inner;          /* sum of inner row lengths (mixed precision with inner rows) */
+    long long inner_builds;     /* inner row rebuilds since import */
+    long long n_inner_wall;     /* sum of inner wall row lengths */
 } gdem_stats;
 
 /* ---- lifecycle ---- */

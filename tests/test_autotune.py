@@ -1,6 +1,5 @@
 """The autotuner's greedy search (host logic, CPU) and, on the GPU, that the
-tuned engine steps the same trajectory as the default one (to FP32
-rounding: the kernel variants are compiled separately)."""
+tuned engine steps the same trajectory as the default one."""
 from __future__ import annotations
 
 import numpy as np
@@ -29,11 +28,12 @@ def test_candidates_keep_the_cell_at_least_the_list_cutoff():
     sc = scenes.config1_box_drop()
     rmax = float(sc.r.max())
     stages = autotune.candidate_stages(sc, "mixed")
-    assert len(stages) == 3
+    assert len(stages) == 4
     for opt in stages[1]:
         assert opt["cell_size"] >= 2 * rmax + opt["skin"] - 1e-15
     assert {o["mixed_kernel"] for o in stages[0]} == {1, 2, 3}
     assert len(autotune.candidate_stages(sc, "fp64")) == 2
+    assert all(o["inner_skin"] > 0 for o in stages[2])
 
 
 @pytest.mark.gpu
@@ -42,12 +42,12 @@ def test_tuned_engine_steps_the_same_trajectory():
     sc = scenes.config2_tilted_box(n=5_000)
     t = autotune.autotune(sc, precision="mixed", model="hertz_mindlin", steps=16, warmup=4)
     assert t.ms_per_step > 0 and len(t.trials) == len(autotune.KERNELS) + len(autotune.SKIN_FACTORS) + len(
-        autotune.GRAPH_STEPS)
+        autotune.INNER_FACTORS) + len(autotune.GRAPH_STEPS)
     A = engine.Engine(sc, precision="mixed", model="hertz_mindlin")
     B = engine.Engine(sc, precision="mixed", model="hertz_mindlin", **t.settings)
     A.step(300)
     B.step(300)
     xa, xb = A.export_positions(), B.export_positions()
-    # skin, cell size and graph length leave the trajectory unchanged; the
-    # kernel variants differ only in how the compiler fused FP32 products
-    assert np.max(np.abs(xa - xb)) <= 1e-5 * float(sc.r.min())
+    # kernel, skin, cell size, inner skin and graph length leave the
+    # trajectory unchanged: the contacts and their order are the same
+    assert np.array_equal(xa, xb)

@@ -108,7 +108,8 @@ def test_mixed_kernels_rebuild_with_fp64_while_pouring():
     rebuilt every few steps.  Every mixed step kernel rebuilds at the steps
     FP64 does: the persistent kernels integrate many particles per thread, and
     every particle's refresh vote counts.  The three kernels step
-    bit-identical trajectories, and a repeat gives the same bits."""
+    bit-identical trajectories, and a repeat gives the same bits, with the
+    inner rows or the list rows scanned."""
     from dataclasses import replace
     from gpudem_gb300 import engine, scenes
     sc = replace(scenes.config3_chute_pour(n=300_000), dt=2e-5, e=0.1)
@@ -125,6 +126,8 @@ def test_mixed_kernels_rebuild_with_fp64_while_pouring():
 
     _, rf = run("fp64")
     runs = [run("mixed", mixed_kernel=k) for k in (1, 2, 3, 1)]
+    # the step scanning the list rows instead of the inner rows
+    runs += [run("mixed", mixed_kernel=k, inner_skin=-1.0) for k in (1, 3)]
     print(f"pour, rebuilds in 600 steps: fp64 {rf}, mixed kernels {[r for _, r in runs]}")
     assert rf >= 10
     for x, rb in runs:
