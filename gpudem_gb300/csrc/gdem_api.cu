@@ -52,6 +52,7 @@ struct MeshData {
     char* arena = nullptr;
     TriRec* rec = nullptr;
     BNode* nodes = nullptr;
+    BNodeF* nodesf = nullptr;  // FP32 copy of the tree (mixed-precision list build)
     double* aabb_d = nullptr;
     uint32_t* morton[2] = {nullptr, nullptr};
     int* idx[2] = {nullptr, nullptr};
@@ -70,7 +71,7 @@ static void launch_bvh_rebuild(const MeshData& M, cudaStream_t st) {
     launch_tri_keys(M.rec, M.morton[0], M.idx[0], M.ntri, M.gmin, M.ginv, st);
     radix_sort_pairs(M.morton[0], M.idx[0], M.morton[1], M.idx[1], M.hist, M.tot, M.ntri, rs_blocks_for(M.ntri), 0,
                      4, st);
-    launch_bvh_build(M.aabb_d, M.nodes, M.morton[0], M.idx[0], M.seg, M.done, M.ntri, st);
+    launch_bvh_build(M.aabb_d, M.nodes, M.nodesf, M.morton[0], M.idx[0], M.seg, M.done, M.ntri, st);
 }
 
 // Everything that depends on the precision mode.
@@ -286,6 +287,7 @@ struct Impl : EngineBase {
         v.ntri = M.ntri;
         v.tri = M.rec;
         v.bvh = M.nodes;
+        v.bvhf = M.nodesf;
         v.bvh_root = 0;
         if (T::mixed) {
             cudaFree(trif);
@@ -1126,6 +1128,7 @@ static int upload_mesh(gdem_handle* h, const std::vector<double>& vx, const std:
     const int nb = rs_blocks_for(T);
     A.add(&M.rec, T);
     A.add(&M.nodes, 2 * (size_t)T);
+    A.add(&M.nodesf, 2 * (size_t)T);
     A.add(&M.aabb_d, 6 * (size_t)T);
     A.add(&dvx, NV); A.add(&dvy, NV); A.add(&dvz, NV);
     A.add(&draw3, raw3_h ? 3 * (size_t)T : (size_t)T);
@@ -1158,7 +1161,7 @@ static int upload_mesh(gdem_handle* h, const std::vector<double>& vx, const std:
         M.ginv[k] = inv[k];
     }
     radix_sort_pairs(M.morton[0], M.idx[0], M.morton[1], M.idx[1], M.hist, M.tot, T, nb, 0, 4, st);
-    launch_bvh_build(M.aabb_d, M.nodes, M.morton[0], M.idx[0], M.seg, M.done, T, st);
+    launch_bvh_build(M.aabb_d, M.nodes, M.nodesf, M.morton[0], M.idx[0], M.seg, M.done, T, st);
     CK(cudaStreamSynchronize(st));
     CK(cudaGetLastError());
     h->eng->set_mesh(M);

@@ -59,6 +59,16 @@ struct __align__(16) BNode {
 };
 static_assert(sizeof(BNode) == 64, "BNode must be 64 bytes");
 
+// FP32 copy of an LBVH node for the mixed-precision list build: the box
+// rounded outwards; children (internal node) or -1 - triangle index (leaf).
+struct __align__(16) BNodeF {
+    float lo[3];
+    int left;
+    float hi[3];
+    int right;
+};
+static_assert(sizeof(BNodeF) == 32, "BNodeF must be 32 bytes");
+
 // Mixed-mode copy of a triangle: the first corner as a float pair, the rest
 // in FP32 (128 bytes).
 struct __align__(16) TriRecF {
@@ -190,6 +200,7 @@ struct View {
     const TriLoF* trilo;             // mixed mode
     float wall_delta;                // mixed mode: bound on the FP32 error of a wall distance (m)
     const BNode* bvh;
+    const BNodeF* bvhf;              // mixed mode: the same tree in FP32
     int ntri;
     int bvh_root;
     // scalars
@@ -398,6 +409,92 @@ __device__ __forceinline__ bool sphere_aabb(double px, double py, double pz, dou
     return (dx * dx + dy * dy + dz * dz) <= Rsq;
 }
 
+// ---------------------------------------------------------------- closest feature, FP32
+struct FeatureF {
+    float nx, ny, nz, dist;
+    int hit;
+    int kind;  // 0 face; 1, 2, 3 corner 0, 1, 2; 4 edge 1-2, 5 edge 0-2, 6 edge 0-1
+    float t;   // edge parameter from the edge's first corner
+};
+
+// Closest feature of triangle T to the sphere centre (ph + pl) within radius^2
+// rsq: the classification of dist_triangle (cpu_dem.cu:12-205) in FP32 on the
+// corner-relative vector.
+__device__ __forceinline__ FeatureF closest_feature_f(float3 ph, float3 pl, float rsq, const TriRecF& T) {
+    FeatureF res;
+    res.nx = res.ny = res.nz = 0.f;
+    res.dist = 1.e10f;
+    res.hit = -2;
+    res.kind = 0;
+    res.t = 0.f;
+    const float ax = (ph.x - T.v0h[0]) + (pl.x - T.v0l[0]);
+    const float ay = (ph.y - T.v0h[1]) + (pl.y - T.v0l[1]);
+    const float az = (ph.z - T.v0h[2]) + (pl.z - T.v0l[2]);
+    const float dist = T.n[0] * ax + T.n[1] * ay + T.n[2] * az;
+    if (dist * dist > rsq) return res;
+    const float d20 = ax * T.e01[0] + ay * T.e01[1] + az * T.e01[2];
+    const float d21 = ax * T.e02[0] + ay * T.e02[1] + az * T.e02[2];
+    const float v = (T.d11 * d20 - T.d01 * d21) * T.denom;
+    const float w = (T.d00 * d21 - T.d01 * d20) * T.denom;
+    const float u = 1.0f - v - w;
+    if (u > 0.f && v > 0.f && w > 0.f) {
+        const float sign = dist < 0.f ? -1.f : 1.f;
+        res.nx = sign * T.n[0];
+        res.ny = sign * T.n[1];
+        res.nz = sign * T.n[2];
+        res.dist = sign * dist;
+        res.hit = -1;
+        return res;
+    }
+    float rx, ry, rz;  // centre minus the closest point
+    int hit, kind;
+    float t = 0.f;
+    if (v <= 0.f && w <= 0.f) {
+        rx = ax; ry = ay; rz = az;
+        hit = T.i0;
+        kind = 1;
+    } else if (u <= 0.f && w <= 0.f) {
+        rx = ax - T.e01[0]; ry = ay - T.e01[1]; rz = az - T.e01[2];
+        hit = T.i1;
+        kind = 2;
+    } else if (u <= 0.f && v <= 0.f) {
+        rx = ax - T.e02[0]; ry = ay - T.e02[1]; rz = az - T.e02[2];
+        hit = T.i2;
+        kind = 3;
+    } else if (u <= 0.f) {
+        const float bx = ax - T.e01[0], by = ay - T.e01[1], bz = az - T.e01[2];
+        t = (bx * T.e12[0] + by * T.e12[1] + bz * T.e12[2]) * T.d22inv;
+        t = fmaxf(0.f, fminf(1.f, t));
+        rx = bx - t * T.e12[0]; ry = by - t * T.e12[1]; rz = bz - t * T.e12[2];
+        hit = T.e1;
+        kind = 4;
+    } else if (v <= 0.f) {
+        t = d21 * T.d11inv;
+        t = fmaxf(0.f, fminf(1.f, t));
+        rx = ax - t * T.e02[0]; ry = ay - t * T.e02[1]; rz = az - t * T.e02[2];
+        hit = T.e2;
+        kind = 5;
+    } else {
+        t = d20 * T.d00inv;
+        t = fmaxf(0.f, fminf(1.f, t));
+        rx = ax - t * T.e01[0]; ry = ay - t * T.e01[1]; rz = az - t * T.e01[2];
+        hit = T.e0;
+        kind = 6;
+    }
+    res.kind = kind;
+    res.t = t;
+    const float dsq = rx * rx + ry * ry + rz * rz;
+    if (dsq < rsq) {
+        const float inv = rsqrtf(dsq);
+        res.dist = dsq * inv;
+        res.nx = rx * inv;
+        res.ny = ry * inv;
+        res.nz = rz * inv;
+    }
+    res.hit = hit;
+    return res;
+}
+
 // "Last block of the grid" election without waiting: every block bumps a
 // counter after its writes; the block that sees gridDim.x-1 runs the epilogue
 // and resets the counter for the next launch.
@@ -436,9 +533,10 @@ void launch_tri_keys(const TriRec* rec, uint32_t* morton, int* idx, int ntri, co
                      const double* invrange, cudaStream_t st);
 // LBVH of the Morton-sorted triangles: leaves, a segment tree of their boxes
 // in `seg` (bvh_scratch_bytes), internal nodes with their boxes.  `done` is a
-// counter that must start at 0 (it is left at 0).
-void launch_bvh_build(const double* aabb, BNode* nodes, const uint32_t* morton_sorted, const int* sorted_idx,
-                      void* seg, unsigned* done, int ntri, cudaStream_t st);
+// counter that must start at 0 (it is left at 0).  `nodesf` (may be null)
+// receives the FP32 copy of every node.
+void launch_bvh_build(const double* aabb, BNode* nodes, BNodeF* nodesf, const uint32_t* morton_sorted,
+                      const int* sorted_idx, void* seg, unsigned* done, int ntri, cudaStream_t st);
 size_t bvh_scratch_bytes(int ntri);
 void launch_tri_precompute(TriRec* rec, uint32_t* morton, int* idx, const double* vx,
                            const double* vy, const double* vz, const int* tv, const int* te,

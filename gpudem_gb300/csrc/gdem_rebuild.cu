@@ -496,6 +496,63 @@ __global__ void __launch_bounds__(kBlock) k_wall_lists(View<T> v, int gated) {
         const SBank<T> S = v.S[s];
         if (S.rot[i].w == 0 || v.ntri == 0) {
             v.nneiw[i] = 0;
+        } else if constexpr (T::mixed) {
+            // FP32 traversal of the FP32 tree (boxes rounded outwards) and the
+            // FP32 closest feature, with the cutoff widened by their error
+            // bounds: the rows hold every triangle within r + skin (and maybe
+            // a few more, which the step's exact overlap turns away), so the
+            // contacts are those of the FP64 rows
+            const float4 h = S.posh[i], l = S.posl[i];
+            const float3 pl = make_float3(l.x, l.y, l.z);
+            const float R = fabsf(h.w) + l.w + (float)v.skin + v.nb_delta + v.wall_delta;
+            const float Rsq = R * R;
+            int cand[CAP];
+            bool overflow = false;
+            int stack[kBvhStack];
+            const int nimg = v.per_x && (h.x + R > v.perf[1] || h.x - R < v.perf[0]) ? 2 : 1;
+            for (int img = 0; img < nimg; img++) {
+                float3 ph = make_float3(h.x, h.y, h.z);
+                if (img == 1) ph.x = h.x + R > v.perf[1] ? h.x - v.Lxh : h.x + v.Lxh;
+                int sp = 0;
+                stack[sp++] = v.bvh_root;
+                while (sp > 0) {
+                    const BNodeF N = v.bvhf[stack[--sp]];
+                    const float dx = fmaxf(fmaxf(N.lo[0] - ph.x, ph.x - N.hi[0]), 0.f);
+                    const float dy = fmaxf(fmaxf(N.lo[1] - ph.y, ph.y - N.hi[1]), 0.f);
+                    const float dz = fmaxf(fmaxf(N.lo[2] - ph.z, ph.z - N.hi[2]), 0.f);
+                    if (!(dx * dx + dy * dy + dz * dz <= Rsq)) continue;
+                    if (N.left < 0) {
+                        const int t = -1 - N.left;
+                        float3 qh = ph, ql = pl;
+                        if (img == 1) ql.x = 0.f;  // the period's low part is within the margin
+                        const FeatureF f = closest_feature_f(qh, ql, Rsq, v.trif[t]);
+                        if (f.dist < R) {
+                            if (count >= CAP) {
+                                overflow = true;
+                                continue;
+                            }
+                            int k = count;
+                            while (k > 0 && cand[k - 1] > t) {
+                                cand[k] = cand[k - 1];
+                                k--;
+                            }
+                            cand[k] = t;
+                            count++;
+                        }
+                    } else {
+                        if (sp + 2 > kBvhStack) {
+                            atomicOr(&ctl->error, 0x10u);
+                            break;
+                        }
+                        stack[sp++] = N.left;
+                        stack[sp++] = N.right;
+                    }
+                }
+            }
+            if (overflow || count > v.wall_cap) atomicOr(&ctl->error, 0x2u);
+            const int m = count < v.wall_cap ? count : v.wall_cap;
+            for (int k = 0; k < m; k++) v.neiw[(size_t)k * n + i] = cand[k];
+            v.nneiw[i] = m;
         } else {
             const double4_32a pi = load_pos(S, i);
             const double py = pi.y, pz = pi.z;
@@ -603,12 +660,21 @@ __global__ void __launch_bounds__(kBlock) k_inner(View<T> v) {
             v.ninn[i] = m < v.nei_cap ? m : v.nei_cap;
             int mw = 0;
             if (hi.w > 0.f && v.ntri > 0) {
-                const double4_32a p = load_pos(S, i);
-                const double R = p.w + v.inner_skin;
+                // FP32 closest feature with the cutoff widened by its error bound
+                const float4 lo = S.posl[i];
+                const float R = hi.w + lo.w + v.inner_skinf + v.nb_delta + v.wall_delta;
                 const int nw = v.nneiw[i];
                 for (int k = 0; k < nw; k++) {
                     const int t = v.neiw[(size_t)k * n + i];
-                    const Feature f = closest_feature(image_x_near(v, p.x, v.tri[t].v0[0]), p.y, p.z, R * R, v.tri[t]);
+                    float3 ph = make_float3(hi.x, hi.y, hi.z), pl = make_float3(lo.x, lo.y, lo.z);
+                    if (v.per_x) {
+                        const float d = ph.x - v.trif[t].v0h[0];
+                        if (d > v.halfLxf || d < -v.halfLxf) {
+                            ph.x = d > 0.f ? ph.x - v.Lxh : ph.x + v.Lxh;
+                            pl.x = 0.f;  // within the margin
+                        }
+                    }
+                    const FeatureF f = closest_feature_f(ph, pl, R * R, v.trif[t]);
                     if (f.dist < R) v.innw[(size_t)mw++ * n + i] = t;
                 }
             }
@@ -830,8 +896,22 @@ __device__ __forceinline__ SegBox seg_load_cg(const SegBox* p) {
 constexpr int kSegTile = 512;
 constexpr int kSegTileLevels = 10;  // levels 0..9 inside one CTA's 512 leaves
 
-__global__ void __launch_bounds__(kSegTile) k_lbvh_leaves(BNode* nodes, const double* aabb, const int* sorted_idx,
-                                                         SegBox* seg, unsigned* done, int n) {
+// FP32 node with its box rounded outwards (nf may be null)
+__device__ __forceinline__ void put_nodef(BNodeF* nf, int i, const double* lo, const double* hi, int left,
+                                          int right) {
+    if (!nf) return;
+    BNodeF F;
+    for (int k = 0; k < 3; k++) {
+        F.lo[k] = __double2float_rd(lo[k]);
+        F.hi[k] = __double2float_ru(hi[k]);
+    }
+    F.left = left;
+    F.right = right;
+    nf[i] = F;
+}
+
+__global__ void __launch_bounds__(kSegTile) k_lbvh_leaves(BNode* nodes, BNodeF* nf, const double* aabb,
+                                                         const int* sorted_idx, SegBox* seg, unsigned* done, int n) {
     __shared__ SegBox sb[kSegTile];
     const int tid = threadIdx.x;
     const int l = blockIdx.x * kSegTile + tid;
@@ -850,6 +930,7 @@ __global__ void __launch_bounds__(kSegTile) k_lbvh_leaves(BNode* nodes, const do
         L.tri = t;
         L.left = L.right = -1;
         L.parent = -1;
+        put_nodef(nf, n - 1 + l, b.lo, b.hi, -1 - t, -1);
         seg[l] = b;
         sb[tid] = b;
     }
@@ -895,7 +976,7 @@ __global__ void __launch_bounds__(kSegTile) k_lbvh_leaves(BNode* nodes, const do
     if (tid == 0) *done = 0u;
 }
 
-__global__ void k_lbvh_internal(BNode* nodes, const uint32_t* key, const SegBox* seg, int n) {
+__global__ void k_lbvh_internal(BNode* nodes, BNodeF* nf, const uint32_t* key, const SegBox* seg, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n - 1) return;
     const int d = (lbvh_delta(key, n, i, i + 1) - lbvh_delta(key, n, i, i - 1)) >= 0 ? 1 : -1;
@@ -943,14 +1024,16 @@ __global__ void k_lbvh_internal(BNode* nodes, const uint32_t* key, const SegBox*
     nodes[left].parent = i;
     nodes[right].parent = i;
     if (i == 0) N.parent = -1;
+    put_nodef(nf, i, box.lo, box.hi, left, right);
 }
 
-void launch_bvh_build(const double* aabb, BNode* nodes, const uint32_t* morton_sorted, const int* sorted_idx,
-                      void* seg, unsigned* done, int ntri, cudaStream_t st) {
+void launch_bvh_build(const double* aabb, BNode* nodes, BNodeF* nodesf, const uint32_t* morton_sorted,
+                      const int* sorted_idx, void* seg, unsigned* done, int ntri, cudaStream_t st) {
     if (ntri <= 0) return;
     SegBox* sg = static_cast<SegBox*>(seg);
-    k_lbvh_leaves<<<(ntri + kSegTile - 1) / kSegTile, kSegTile, 0, st>>>(nodes, aabb, sorted_idx, sg, done, ntri);
-    if (ntri > 1) k_lbvh_internal<<<grid_for(ntri - 1), kBlock, 0, st>>>(nodes, morton_sorted, sg, ntri);
+    k_lbvh_leaves<<<(ntri + kSegTile - 1) / kSegTile, kSegTile, 0, st>>>(nodes, nodesf, aabb, sorted_idx, sg, done,
+                                                                         ntri);
+    if (ntri > 1) k_lbvh_internal<<<grid_for(ntri - 1), kBlock, 0, st>>>(nodes, nodesf, morton_sorted, sg, ntri);
 }
 
 // the segment tree's nodes: every level up to the root, and at least the

@@ -29,91 +29,6 @@ namespace gdem {
 
 namespace {
 
-struct FeatureF {
-    float nx, ny, nz, dist;
-    int hit;
-    int kind;  // 0 face; 1, 2, 3 corner 0, 1, 2; 4 edge 1-2, 5 edge 0-2, 6 edge 0-1
-    float t;   // edge parameter from the edge's first corner
-};
-
-// Closest feature of triangle T to the sphere centre (ph + pl) within radius^2
-// rsq: the classification of dist_triangle (cpu_dem.cu:12-205) in FP32 on the
-// corner-relative vector.
-__device__ __forceinline__ FeatureF closest_feature_f(float3 ph, float3 pl, float rsq, const TriRecF& T) {
-    FeatureF res;
-    res.nx = res.ny = res.nz = 0.f;
-    res.dist = 1.e10f;
-    res.hit = -2;
-    res.kind = 0;
-    res.t = 0.f;
-    const float ax = (ph.x - T.v0h[0]) + (pl.x - T.v0l[0]);
-    const float ay = (ph.y - T.v0h[1]) + (pl.y - T.v0l[1]);
-    const float az = (ph.z - T.v0h[2]) + (pl.z - T.v0l[2]);
-    const float dist = T.n[0] * ax + T.n[1] * ay + T.n[2] * az;
-    if (dist * dist > rsq) return res;
-    const float d20 = ax * T.e01[0] + ay * T.e01[1] + az * T.e01[2];
-    const float d21 = ax * T.e02[0] + ay * T.e02[1] + az * T.e02[2];
-    const float v = (T.d11 * d20 - T.d01 * d21) * T.denom;
-    const float w = (T.d00 * d21 - T.d01 * d20) * T.denom;
-    const float u = 1.0f - v - w;
-    if (u > 0.f && v > 0.f && w > 0.f) {
-        const float sign = dist < 0.f ? -1.f : 1.f;
-        res.nx = sign * T.n[0];
-        res.ny = sign * T.n[1];
-        res.nz = sign * T.n[2];
-        res.dist = sign * dist;
-        res.hit = -1;
-        return res;
-    }
-    float rx, ry, rz;  // centre minus the closest point
-    int hit, kind;
-    float t = 0.f;
-    if (v <= 0.f && w <= 0.f) {
-        rx = ax; ry = ay; rz = az;
-        hit = T.i0;
-        kind = 1;
-    } else if (u <= 0.f && w <= 0.f) {
-        rx = ax - T.e01[0]; ry = ay - T.e01[1]; rz = az - T.e01[2];
-        hit = T.i1;
-        kind = 2;
-    } else if (u <= 0.f && v <= 0.f) {
-        rx = ax - T.e02[0]; ry = ay - T.e02[1]; rz = az - T.e02[2];
-        hit = T.i2;
-        kind = 3;
-    } else if (u <= 0.f) {
-        const float bx = ax - T.e01[0], by = ay - T.e01[1], bz = az - T.e01[2];
-        t = (bx * T.e12[0] + by * T.e12[1] + bz * T.e12[2]) * T.d22inv;
-        t = fmaxf(0.f, fminf(1.f, t));
-        rx = bx - t * T.e12[0]; ry = by - t * T.e12[1]; rz = bz - t * T.e12[2];
-        hit = T.e1;
-        kind = 4;
-    } else if (v <= 0.f) {
-        t = d21 * T.d11inv;
-        t = fmaxf(0.f, fminf(1.f, t));
-        rx = ax - t * T.e02[0]; ry = ay - t * T.e02[1]; rz = az - t * T.e02[2];
-        hit = T.e2;
-        kind = 5;
-    } else {
-        t = d20 * T.d00inv;
-        t = fmaxf(0.f, fminf(1.f, t));
-        rx = ax - t * T.e01[0]; ry = ay - t * T.e01[1]; rz = az - t * T.e01[2];
-        hit = T.e0;
-        kind = 6;
-    }
-    res.kind = kind;
-    res.t = t;
-    const float dsq = rx * rx + ry * ry + rz * rz;
-    if (dsq < rsq) {
-        const float inv = rsqrtf(dsq);
-        res.dist = dsq * inv;
-        res.nx = rx * inv;
-        res.ny = ry * inv;
-        res.nz = rz * inv;
-    }
-    res.hit = hit;
-    return res;
-}
-
 // (hi, lo) += d with an error-free sum (Knuth's TwoSum, then a fast
 // renormalisation).  Intrinsic adds: no multiply may be contracted into them.
 __device__ __forceinline__ void pair_add(float& hi, float& lo, float d) {
