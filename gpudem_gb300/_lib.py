@@ -22,7 +22,8 @@ EXPORTED = [
     "gdem_export_lists", "gdem_morton_keys", "gdem_export_cells", "gdem_sort_keys",
     "gdem_sort_keys_noalloc", "gdem_set_mesh_indexed", "gdem_set_particle_materials",
     "gdem_dist_triangle", "gdem_export_mesh", "gdem_get_stream", "gdem_profile_step",
-    "gdem_export_positions",
+    "gdem_export_positions", "gdem_frame_write_async", "gdem_frames_flush", "gdem_save_snapshot",
+    "gdem_load_snapshot",
 ]
 
 
@@ -122,6 +123,10 @@ def load(build_if_missing: bool = False):
     L.gdem_get_stream.argtypes = [vp, C.POINTER(vp)]
     L.gdem_export_positions.argtypes = [vp, vp]
     L.gdem_profile_step.argtypes = [vp, C.c_int, C.POINTER(C.c_float)]
+    L.gdem_frame_write_async.argtypes = [vp, C.c_char_p, C.c_int, C.c_double]
+    L.gdem_frames_flush.argtypes = [vp]
+    L.gdem_save_snapshot.argtypes = [vp, C.c_char_p]
+    L.gdem_load_snapshot.argtypes = [vp, C.c_char_p]
     for nm in EXPORTED:
         if nm != "gdem_last_error":
             getattr(L, nm).restype = C.c_int

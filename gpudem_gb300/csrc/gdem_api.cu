@@ -10,8 +10,13 @@
 
 #include <algorithm>
 #include <cmath>
+#include <condition_variable>
+#include <deque>
 #include <memory>
+#include <mutex>
 #include <string>
+#include <thread>
+#include <type_traits>
 #include <unordered_map>
 #include <vector>
 
@@ -90,6 +95,10 @@ struct EngineBase {
     virtual int set_materials(const double* mu, const double* restitution) = 0;
     virtual void set_mesh(const MeshData& m) = 0;
     virtual unsigned error_word() = 0;
+    virtual int frame_async(const char* dir, int step, double length_factor) = 0;
+    virtual int frames_flush() = 0;
+    virtual int save_snapshot(const char* path) = 0;
+    virtual int load_snapshot(const char* path) = 0;
     std::string err;
     cudaStream_t st = nullptr;
     bool imported = false;
@@ -124,6 +133,7 @@ struct Impl : EngineBase {
     bool use_graphs = true;
 
     ~Impl() override {
+        frames_shutdown();
         if (st) cudaStreamSynchronize(st);
         destroy_graphs();
         cudaFree(arena);
@@ -869,6 +879,408 @@ struct Impl : EngineBase {
         return GDEM_OK;
     }
 
+    // ---------------------------------------------------------------- frames
+    // write_frame_bin payloads built on the device (gdem_output.cu), copied to
+    // pinned host buffers on a copy stream after the frame kernels, and
+    // written to files by a host thread: the steps launched after a frame run
+    // while it travels and lands.  Three buffers; a fourth frame waits for one.
+    struct FrameSlot {
+        char* dev = nullptr;
+        char* host = nullptr;
+        cudaEvent_t ready = nullptr, copied = nullptr;
+        bool busy = false;
+    };
+    struct FrameJob {
+        int slot;
+        std::string path;
+    };
+    static constexpr int kFrameSlots = 3;
+    FrameSlot fslot[kFrameSlots];
+    void* fscratch = nullptr;
+    cudaStream_t copy_st = nullptr;
+    std::thread fwriter;
+    std::mutex fmu;
+    std::condition_variable fcv;
+    std::deque<FrameJob> fjobs;
+    bool fstop = false;
+    int fpending = 0;
+    std::string ferr;
+
+    int frames_init() {
+        if (fscratch) return GDEM_OK;
+        CKE(cudaMalloc(&fscratch, frame_scratch_bytes(n)));
+        CKE(cudaStreamCreateWithFlags(&copy_st, cudaStreamNonBlocking));
+        const size_t fb = frame_bytes(n);
+        for (auto& s : fslot) {
+            CKE(cudaMalloc((void**)&s.dev, fb));
+            CKE(cudaHostAlloc((void**)&s.host, fb, cudaHostAllocDefault));
+            CKE(cudaEventCreateWithFlags(&s.ready, cudaEventDisableTiming));
+            CKE(cudaEventCreateWithFlags(&s.copied, cudaEventDisableTiming));
+        }
+        fwriter = std::thread([this] { frame_writer(); });
+        return GDEM_OK;
+    }
+
+    void frame_writer() {
+        for (;;) {
+            FrameJob job;
+            {
+                std::unique_lock<std::mutex> lk(fmu);
+                fcv.wait(lk, [this] { return fstop || !fjobs.empty(); });
+                if (fjobs.empty()) return;
+                job = fjobs.front();
+                fjobs.pop_front();
+            }
+            FrameSlot& s = fslot[job.slot];
+            std::string e;
+            if (cudaEventSynchronize(s.copied) != cudaSuccess) {
+                e = "frame copy failed";
+            } else {
+                int count = 0;
+                memcpy(&count, s.host, 4);
+                FILE* fp = fopen(job.path.c_str(), "wb");
+                if (!fp) {
+                    e = "cannot open " + job.path;
+                } else {
+                    const size_t bytes = 4 + 16 * (size_t)count;
+                    if (fwrite(s.host, 1, bytes, fp) != bytes) e = "short write to " + job.path;
+                    if (fclose(fp) != 0 && e.empty()) e = "cannot close " + job.path;
+                }
+            }
+            {
+                std::lock_guard<std::mutex> lk(fmu);
+                if (!e.empty() && ferr.empty()) ferr = e;
+                s.busy = false;
+                fpending--;
+            }
+            fcv.notify_all();
+        }
+    }
+
+    void frames_shutdown() {
+        if (!fscratch) return;
+        {
+            std::lock_guard<std::mutex> lk(fmu);
+            fstop = true;
+        }
+        fcv.notify_all();
+        if (fwriter.joinable()) fwriter.join();
+        for (auto& s : fslot) {
+            cudaFree(s.dev);
+            cudaFreeHost(s.host);
+            if (s.ready) cudaEventDestroy(s.ready);
+            if (s.copied) cudaEventDestroy(s.copied);
+        }
+        cudaFree(fscratch);
+        fscratch = nullptr;
+        if (copy_st) cudaStreamDestroy(copy_st);
+    }
+
+    int frame_async(const char* dir, int step, double lf) override {
+        if (!dir) return failv(err, GDEM_ERR_ARG, "frame: null directory");
+        int rc = frames_init();
+        if (rc) return rc;
+        int k = -1;
+        {
+            std::unique_lock<std::mutex> lk(fmu);
+            fcv.wait(lk, [this] {
+                for (auto& s : fslot)
+                    if (!s.busy) return true;
+                return false;
+            });
+            for (int q = 0; q < kFrameSlots && k < 0; q++)
+                if (!fslot[q].busy) k = q;
+            fslot[k].busy = true;
+            fpending++;
+        }
+        FrameSlot& s = fslot[k];
+        launch_frame(v, fscratch, s.dev, lf, st);
+        cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaEventRecord(s.ready, st);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(copy_st, s.ready, 0);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(s.host, s.dev, frame_bytes(n), cudaMemcpyDeviceToHost, copy_st);
+        if (e == cudaSuccess) e = cudaEventRecord(s.copied, copy_st);
+        if (e != cudaSuccess) {
+            {
+                std::lock_guard<std::mutex> lk(fmu);
+                s.busy = false;
+                fpending--;
+            }
+            fcv.notify_all();
+            return failv(err, GDEM_ERR_CUDA, std::string("frame: ") + cudaGetErrorString(e));
+        }
+        char name[64];
+        snprintf(name, sizeof(name), "/result_%012d.bin", step);
+        {
+            std::lock_guard<std::mutex> lk(fmu);
+            fjobs.push_back(FrameJob{k, std::string(dir) + name});
+        }
+        fcv.notify_all();
+        return GDEM_OK;
+    }
+
+    int frames_flush() override {
+        std::string e;
+        {
+            std::unique_lock<std::mutex> lk(fmu);
+            fcv.wait(lk, [this] { return fpending == 0; });
+            e.swap(ferr);
+        }
+        if (!e.empty()) return failv(err, GDEM_ERR_ARG, e);
+        return GDEM_OK;
+    }
+
+    // ---------------------------------------------------------------- snapshot
+    // The exact state in pId order: the precision's own representation of
+    // positions, velocities, spins (float pairs in mixed mode) and material
+    // records, and the compact contact histories with partners as pIds (all
+    // spring terms).  Loading it into an engine of the same size, precision
+    // and model (with its mesh set) continues the run bit for bit: storage
+    // order, lists and rebuild times differ, and none of them enters the
+    // results.
+    struct SnapHeader {
+        char magic[8];
+        int version, n, precision, model, hist_cap, histw_cap, per_particle_mat, rsize;
+        unsigned long long steps;
+        unsigned error, pad;
+    };
+
+    int save_snapshot(const char* path) override {
+        if (!path) return failv(err, GDEM_ERR_ARG, "snapshot: null path");
+        Ctl c;
+        std::vector<int> pid;
+        int rc = current(c, pid);
+        if (rc) return rc;
+        const SBank<T>& S = v.S[c.s];
+        const PBank<T>& P = v.P[c.p];
+        const int H = v.hist_cap, HW = v.histw_cap;
+        std::vector<int> at(n);
+        for (int i = 0; i < n; i++) at[pid[i]] = i;
+        std::vector<V4> vel, rot, mat;
+        std::vector<double4_32a> pos;
+        std::vector<float4> ph, pl, vl, wl;
+        std::vector<int> nc, ncw, hid, hwid;
+        std::vector<R> hh[6], hw[6];
+        if ((rc = dl(vel, S.vel, n)) || (rc = dl(rot, S.rot, n)) || (rc = dl(mat, P.mat, n)) ||
+            (rc = dl(nc, P.nc, n)) || (rc = dl(ncw, P.ncw, n)) || (rc = dl(hid, P.hid, (size_t)n * H)) ||
+            (rc = dl(hwid, P.hwid, (size_t)n * HW)))
+            return rc;
+        R* const hsrc[6] = {P.hx, P.hy, P.hz, P.cx, P.cy, P.cz};
+        R* const wsrc[6] = {P.hwx, P.hwy, P.hwz, P.cwx, P.cwy, P.cwz};
+        const int nterms = T::mixed ? 6 : 3;
+        for (int a = 0; a < nterms; a++)
+            if ((rc = dl(hh[a], hsrc[a], (size_t)n * H)) || (rc = dl(hw[a], wsrc[a], (size_t)n * HW))) return rc;
+        if (T::mixed) {
+            if ((rc = dl(ph, S.posh, n)) || (rc = dl(pl, S.posl, n)) || (rc = dl(vl, S.vell, n)) ||
+                (rc = dl(wl, S.rotl, n)))
+                return rc;
+        } else if ((rc = dl(pos, S.pos, n))) {
+            return rc;
+        }
+        FILE* fp = fopen(path, "wb");
+        if (!fp) return failv(err, GDEM_ERR_ARG, std::string("snapshot: cannot open ") + path);
+        bool ok = true;
+        auto put = [&](const void* p, size_t bytes) {
+            if (ok && fwrite(p, 1, bytes, fp) != bytes) ok = false;
+        };
+        SnapHeader hd;
+        memset(&hd, 0, sizeof(hd));
+        memcpy(hd.magic, "GDEMSNAP", 8);
+        hd.version = 1;
+        hd.n = n;
+        hd.precision = T::mixed ? GDEM_MIXED : GDEM_FP64;
+        hd.model = d.model;
+        hd.hist_cap = H;
+        hd.histw_cap = HW;
+        hd.per_particle_mat = v.per_particle_mat;
+        hd.rsize = (int)sizeof(R);
+        hd.steps = c.steps;
+        hd.error = c.error;
+        put(&hd, sizeof(hd));
+        auto put_perm = [&](const auto& a) {
+            using E = typename std::decay<decltype(a)>::type::value_type;
+            std::vector<E> o(n);
+            for (int q = 0; q < n; q++) o[q] = a[at[q]];
+            put(o.data(), sizeof(E) * o.size());
+        };
+        if (T::mixed) {
+            put_perm(ph); put_perm(pl); put_perm(vel); put_perm(vl); put_perm(rot); put_perm(wl);
+        } else {
+            put_perm(pos); put_perm(vel); put_perm(rot);
+        }
+        put_perm(mat);
+        // histories: counts, then each particle's live entries (partner pId or
+        // triangle, then the spring terms)
+        auto put_hist = [&](const std::vector<int>& cnt, const std::vector<int>& id, std::vector<R>* terms,
+                            bool partner_is_particle) {
+            put_perm(cnt);
+            std::vector<int> ids;
+            std::vector<R> vals;
+            for (int q = 0; q < n; q++) {
+                const int i = at[q];
+                for (int k = 0; k < cnt[i]; k++) {
+                    const size_t s = (size_t)k * n + i;
+                    int key = id[s];
+                    if (partner_is_particle && T::mixed) key = pid[key];  // storage index -> pId
+                    ids.push_back(key);
+                    for (int a = 0; a < nterms; a++) vals.push_back(terms[a][s]);
+                }
+            }
+            put(ids.data(), sizeof(int) * ids.size());
+            put(vals.data(), sizeof(R) * vals.size());
+        };
+        put_hist(nc, hid, hh, true);
+        put_hist(ncw, hwid, hw, false);
+        if (fclose(fp) != 0) ok = false;
+        if (!ok) return failv(err, GDEM_ERR_ARG, std::string("snapshot: cannot write ") + path);
+        return GDEM_OK;
+    }
+
+    int load_snapshot(const char* path) override {
+        if (!path) return failv(err, GDEM_ERR_ARG, "snapshot: null path");
+        FILE* fp = fopen(path, "rb");
+        if (!fp) return failv(err, GDEM_ERR_ARG, std::string("snapshot: cannot open ") + path);
+        bool ok = true;
+        auto get = [&](void* p, size_t bytes) {
+            if (ok && fread(p, 1, bytes, fp) != bytes) ok = false;
+        };
+        SnapHeader hd;
+        get(&hd, sizeof(hd));
+        const int H = v.hist_cap, HW = v.histw_cap;
+        if (!ok || memcmp(hd.magic, "GDEMSNAP", 8) != 0 || hd.version != 1) {
+            fclose(fp);
+            return failv(err, GDEM_ERR_ARG, "snapshot: not a snapshot file");
+        }
+        if (hd.n != n || hd.precision != (T::mixed ? GDEM_MIXED : GDEM_FP64) || hd.model != d.model ||
+            hd.rsize != (int)sizeof(R)) {
+            fclose(fp);
+            return failv(err, GDEM_ERR_ARG, "snapshot: size, precision or model differs from this engine");
+        }
+        std::vector<V4> vel(n), rot(n), mat(n);
+        std::vector<double4_32a> pos;
+        std::vector<float4> ph, pl, vl, wl;
+        if (T::mixed) {
+            ph.resize(n); pl.resize(n); vl.resize(n); wl.resize(n);
+            get(ph.data(), 16 * (size_t)n); get(pl.data(), 16 * (size_t)n);
+            get(vel.data(), sizeof(V4) * (size_t)n); get(vl.data(), 16 * (size_t)n);
+            get(rot.data(), sizeof(V4) * (size_t)n); get(wl.data(), 16 * (size_t)n);
+        } else {
+            pos.resize(n);
+            get(pos.data(), sizeof(double4_32a) * (size_t)n);
+            get(vel.data(), sizeof(V4) * (size_t)n);
+            get(rot.data(), sizeof(V4) * (size_t)n);
+        }
+        get(mat.data(), sizeof(V4) * (size_t)n);
+        const int nterms = T::mixed ? 6 : 3;
+        std::vector<int> nc(n), ncw(n), ids, idsw;
+        std::vector<R> vals, valsw;
+        auto get_hist = [&](std::vector<int>& cnt, std::vector<int>& id, std::vector<R>& val, int cap) {
+            get(cnt.data(), sizeof(int) * (size_t)n);
+            size_t tot = 0;
+            for (int q = 0; q < n && ok; q++) {
+                if (cnt[q] < 0 || cnt[q] > cap) ok = false;
+                tot += (size_t)cnt[q];
+            }
+            if (!ok) return;
+            id.resize(tot);
+            val.resize(tot * nterms);
+            get(id.data(), sizeof(int) * tot);
+            get(val.data(), sizeof(R) * val.size());
+        };
+        get_hist(nc, ids, vals, H);
+        get_hist(ncw, idsw, valsw, HW);
+        fclose(fp);
+        if (!ok) return failv(err, GDEM_ERR_ARG, "snapshot: truncated, or a history longer than this engine's capacity");
+        // set the engine up as an import would (grid, lists), from the
+        // reference-layout view of the snapshot ...
+        std::vector<double> x(3 * (size_t)n), vv(3 * (size_t)n), ww(3 * (size_t)n), r(n), m(n), k(n), eta(n);
+        std::vector<int> act(n);
+        for (int q = 0; q < n; q++) {
+            double xs[4];
+            if (T::mixed) {
+                xs[0] = (double)ph[q].x + (double)pl[q].x;
+                xs[1] = (double)ph[q].y + (double)pl[q].y;
+                xs[2] = (double)ph[q].z + (double)pl[q].z;
+                xs[3] = (double)fabsf(ph[q].w) + (double)pl[q].w;
+            } else {
+                xs[0] = pos[q].x; xs[1] = pos[q].y; xs[2] = pos[q].z; xs[3] = pos[q].w;
+            }
+            for (int a = 0; a < 3; a++) x[3 * q + a] = xs[a];
+            r[q] = xs[3];
+            vv[3 * q] = (double)vel[q].x; vv[3 * q + 1] = (double)vel[q].y; vv[3 * q + 2] = (double)vel[q].z;
+            ww[3 * q] = (double)rot[q].x; ww[3 * q + 1] = (double)rot[q].y; ww[3 * q + 2] = (double)rot[q].z;
+            m[q] = 1. / (double)vel[q].w;
+            k[q] = (double)mat[q].x;
+            eta[q] = (double)mat[q].y;
+            act[q] = rot[q].w == R(1) ? 1 : 0;
+        }
+        gdem_particles pp;
+        memset(&pp, 0, sizeof(pp));
+        pp.n = n;
+        pp.x = x.data(); pp.v = vv.data(); pp.angv = ww.data(); pp.r = r.data(); pp.m = m.data();
+        pp.k = k.data(); pp.etaconst = eta.data(); pp.isActive = act.data();
+        int rc = import_(&pp);
+        if (rc) return rc;
+        // ... then put the exact state into the current banks, in the storage
+        // order the import's rebuild chose
+        Ctl c;
+        std::vector<int> pid;
+        if ((rc = current(c, pid))) return rc;
+        std::vector<int> at(n);
+        for (int i = 0; i < n; i++) at[pid[i]] = i;
+        const SBank<T>& S = v.S[c.s];
+        const PBank<T>& P = v.P[c.p];
+        auto up_perm = [&](auto* dst, const auto& a) -> int {
+            using E = typename std::decay<decltype(a)>::type::value_type;
+            std::vector<E> o(n);
+            for (int q = 0; q < n; q++) o[at[q]] = a[q];
+            CKE(cudaMemcpy(dst, o.data(), sizeof(E) * (size_t)n, cudaMemcpyHostToDevice));
+            return GDEM_OK;
+        };
+        if (T::mixed) {
+            if ((rc = up_perm(S.posh, ph)) || (rc = up_perm(S.posl, pl)) || (rc = up_perm(S.vell, vl)) ||
+                (rc = up_perm(S.rotl, wl)))
+                return rc;
+        } else if ((rc = up_perm(S.pos, pos))) {
+            return rc;
+        }
+        if ((rc = up_perm(S.vel, vel)) || (rc = up_perm(S.rot, rot)) || (rc = up_perm(P.mat, mat))) return rc;
+        auto up_hist = [&](const std::vector<int>& cnt, const std::vector<int>& id, const std::vector<R>& val,
+                           int cap, int* dcnt, int* did, R* const* dterm, bool partner_is_particle) -> int {
+            std::vector<int> c2(n, 0), id2((size_t)n * cap, -1);
+            std::vector<R> t2[6];
+            for (int a = 0; a < nterms; a++) t2[a].assign((size_t)n * cap, R(0));
+            size_t e = 0;
+            for (int q = 0; q < n; q++) {
+                const int i = at[q];
+                c2[i] = cnt[q];
+                for (int kk = 0; kk < cnt[q]; kk++, e++) {
+                    const size_t s = (size_t)kk * n + i;
+                    int key = id[e];
+                    if (partner_is_particle && T::mixed) key = at[key];  // pId -> storage index
+                    id2[s] = key;
+                    for (int a = 0; a < nterms; a++) t2[a][s] = val[e * nterms + a];
+                }
+            }
+            CKE(cudaMemcpy(dcnt, c2.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice));
+            CKE(cudaMemcpy(did, id2.data(), sizeof(int) * id2.size(), cudaMemcpyHostToDevice));
+            for (int a = 0; a < nterms; a++)
+                CKE(cudaMemcpy(dterm[a], t2[a].data(), sizeof(R) * t2[a].size(), cudaMemcpyHostToDevice));
+            return GDEM_OK;
+        };
+        R* const hdst[6] = {P.hx, P.hy, P.hz, P.cx, P.cy, P.cz};
+        R* const wdst[6] = {P.hwx, P.hwy, P.hwz, P.cwx, P.cwy, P.cwz};
+        if ((rc = up_hist(nc, ids, vals, H, P.nc, P.hid, hdst, true)) ||
+            (rc = up_hist(ncw, idsw, valsw, HW, P.ncw, P.hwid, wdst, false)))
+            return rc;
+        v.per_particle_mat = hd.per_particle_mat;
+        destroy_graphs();
+        c.steps = hd.steps;
+        c.error = hd.error;
+        CKE(cudaMemcpy(v.ctl, &c, sizeof(Ctl), cudaMemcpyHostToDevice));
+        return rebuild();
+    }
+
     int profile(int iters, float* avg_ms) override {
         // groups of kProfileBurst launches back to back between two events;
         // the device-gated rebuild runs after each group
@@ -1243,6 +1655,30 @@ int gdem_export_particles(gdem_handle* h, gdem_particles* p) {
     if (!h || !p || p->n != h->d.n_particles) return fail(h, GDEM_ERR_ARG, "export: wrong n");
     if (!h->eng->imported) return fail(h, GDEM_ERR_STATE, "export before import");
     return pass(h, h->eng->export_(p));
+}
+
+int gdem_frame_write_async(gdem_handle* h, const char* dir, int step, double length_factor) {
+    if (!h || !dir) return fail(h, GDEM_ERR_ARG, "frame_write_async: null");
+    if (!h->eng->imported) return fail(h, GDEM_ERR_STATE, "frame before import");
+    return pass(h, h->eng->frame_async(dir, step, length_factor));
+}
+
+int gdem_frames_flush(gdem_handle* h) {
+    if (!h) return GDEM_ERR_ARG;
+    return pass(h, h->eng->frames_flush());
+}
+
+int gdem_save_snapshot(gdem_handle* h, const char* path) {
+    if (!h || !path) return fail(h, GDEM_ERR_ARG, "save_snapshot: null");
+    if (!h->eng->imported) return fail(h, GDEM_ERR_STATE, "snapshot before import");
+    return pass(h, h->eng->save_snapshot(path));
+}
+
+int gdem_load_snapshot(gdem_handle* h, const char* path) {
+    if (!h || !path) return fail(h, GDEM_ERR_ARG, "load_snapshot: null");
+    const int rc = pass(h, h->eng->load_snapshot(path));
+    if (rc == GDEM_OK) h->eng->imported = true;
+    return rc;
 }
 
 int gdem_export_positions(gdem_handle* h, double* x) {

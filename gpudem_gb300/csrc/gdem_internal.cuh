@@ -548,6 +548,11 @@ int rs_blocks_for(int n);
 void launch_dist_triangle(const TriRec* tri, const double* pos, const double* r, const int* t, int m,
                           double* out4, int* hit, cudaStream_t st);
 void launch_trif(const TriRec* tri, TriRecF* out, TriLoF* lo, int ntri, cudaStream_t st);
+// output frames (gdem_output.cu): write_frame_bin's payload built on the device
+size_t frame_scratch_bytes(int n);
+size_t frame_bytes(int n);
+template <class T>
+void launch_frame(const View<T>& v, void* scratch, char* frame, double length_factor, cudaStream_t st);
 // inner rows (mixed mode with inner rows; gated on ctl->irefresh)
 template <class T>
 void launch_inner(const View<T>& v, cudaStream_t st);

@@ -11,6 +11,7 @@ libgdem.so and keeps the reference's index space (pId) at its boundary.
 from __future__ import annotations
 
 import ctypes as C
+import os
 
 import numpy as np
 
@@ -264,6 +265,25 @@ class Engine:
         s = C.c_void_p()
         self._check(self.L.gdem_get_stream(self.h, C.byref(s)), "gdem_get_stream")
         return int(s.value or 0)
+
+    def frame_write_async(self, directory, step, length_factor=1.0):
+        """Queue write_frame_bin's file <directory>/result_%012d.bin of the
+        current state (built on the device, written by a host thread); returns
+        at once.  `frames_flush` waits for the files."""
+        self._check(self.L.gdem_frame_write_async(self.h, os.fsencode(directory), int(step), float(length_factor)),
+                    "gdem_frame_write_async")
+
+    def frames_flush(self):
+        self._check(self.L.gdem_frames_flush(self.h), "gdem_frames_flush")
+
+    def save_snapshot(self, path):
+        """Checkpoint the exact state (see gdem_save_snapshot)."""
+        self._check(self.L.gdem_save_snapshot(self.h, os.fsencode(path)), "gdem_save_snapshot")
+
+    def load_snapshot(self, path):
+        """Restart from a snapshot of an engine of the same size, precision and
+        model; the run continues bit for bit."""
+        self._check(self.L.gdem_load_snapshot(self.h, os.fsencode(path)), "gdem_load_snapshot")
 
     def profile_step(self, iters=10) -> float:
         """Mean duration (ms) of the step kernel alone over `iters` launches."""

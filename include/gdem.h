@@ -209,6 +209,27 @@ int gdem_export_particles(gdem_handle* h, gdem_particles* p);
  * writes every output step, solver_output.cu:259): gathered on the device and
  * copied with one transfer. */
 int gdem_export_positions(gdem_handle* h, double* x);
+
+/* ---- output frames and snapshots ---- */
+/* Queue the current state's output frame, the file write_frame_bin writes
+ * (solver_output.cu:259-316, main.cu:276-286): <dir>/result_%012d.bin with the
+ * int32 count of active particles, their float32 positions times
+ * length_factor, then their float32 radii times length_factor, in pId order.
+ * The frame is built on the device and copied to pinned host memory on a copy
+ * stream; a host thread writes the file.  Returns at once: steps launched
+ * afterwards run while the frame travels (three frames in flight at most).
+ * Replaces copyFromDevice + write_frame_bin at an output step. */
+int gdem_frame_write_async(gdem_handle* h, const char* dir, int step, double length_factor);
+/* Wait until every queued frame is in its file; reports the first failure. */
+int gdem_frames_flush(gdem_handle* h);
+/* Checkpoint: the exact state (the precision's own representation, contact
+ * histories with every spring term), in pId order, to `path`.  No reference
+ * counterpart. */
+int gdem_save_snapshot(gdem_handle* h, const char* path);
+/* Restart: load a snapshot into an engine created with the same particle
+ * count, precision and model, with its mesh set; the run continues bit for
+ * bit as if it had not stopped. */
+int gdem_load_snapshot(gdem_handle* h, const char* path);
 int gdem_stats_get(gdem_handle* h, gdem_stats* s);
 
 /* ---- the hot-path stages, callable one at a time ---- */
