@@ -34,6 +34,7 @@ UNITS = {
     "gdem_stats.cu": True,
     "gdem_noalloc.cu": True,
     "gdem_output.cu": True,
+    "gdem_init.cu": True,
 }
 # the mixed-precision step: FP32 contact law with the hardware's approximate
 # reciprocal and square root (its error is measured against the FP64 mode)

@@ -23,8 +23,19 @@ EXPORTED = [
     "gdem_sort_keys_noalloc", "gdem_set_mesh_indexed", "gdem_set_particle_materials",
     "gdem_dist_triangle", "gdem_export_mesh", "gdem_get_stream", "gdem_profile_step",
     "gdem_export_positions", "gdem_frame_write_async", "gdem_frames_flush", "gdem_save_snapshot",
-    "gdem_load_snapshot",
+    "gdem_load_snapshot", "gdem_init_particles",
 ]
+PLACE = {"random": 0, "lattice": 1}
+RADIUS = {"mono": 0, "uniform": 1, "lognormal": 2, "bidisperse": 3}
+
+
+class Inlet(C.Structure):
+    """gdem_inlet: device-side particle placement (the reference's shuffle inlet)."""
+    _fields_ = [("box_min", C.c_double * 3), ("box_max", C.c_double * 3), ("placement", C.c_int),
+                ("radius_dist", C.c_int), ("r_a", C.c_double), ("r_b", C.c_double), ("r_c", C.c_double),
+                ("r_d", C.c_double), ("density", C.c_double), ("youngs_modulus", C.c_double),
+                ("restitution", C.c_double), ("velocity", C.c_double * 3), ("velocity_sigma", C.c_double),
+                ("gap", C.c_double), ("seed", C.c_ulonglong)]
 
 
 class MeshArrays(C.Structure):
@@ -127,6 +138,7 @@ def load(build_if_missing: bool = False):
     L.gdem_frames_flush.argtypes = [vp]
     L.gdem_save_snapshot.argtypes = [vp, C.c_char_p]
     L.gdem_load_snapshot.argtypes = [vp, C.c_char_p]
+    L.gdem_init_particles.argtypes = [vp, C.POINTER(Inlet)]
     for nm in EXPORTED:
         if nm != "gdem_last_error":
             getattr(L, nm).restype = C.c_int

@@ -98,6 +98,7 @@ struct EngineBase {
     virtual int frame_async(const char* dir, int step, double length_factor) = 0;
     virtual int frames_flush() = 0;
     virtual int save_snapshot(const char* path) = 0;
+    virtual int init_particles(const gdem_inlet* in) = 0;
     virtual int load_snapshot(const char* path) = 0;
     std::string err;
     cudaStream_t st = nullptr;
@@ -411,6 +412,51 @@ struct Impl : EngineBase {
         return x;
     }
 
+    // Grid, skins and refresh thresholds from the largest radius
+    // (initialize_BoundingBox, BoundingBox.cu:370-396).
+    int setup_grid(double rmax) {
+        const double cell = d.cell_size > 0 ? d.cell_size : rmax * 4.;
+        const double skin = d.skin > 0 ? d.skin : rmax;
+        const double thresh = d.refresh_thresh > 0 ? d.refresh_thresh : (d.skin > 0 ? skin * 0.5 : rmax * 0.5);
+        if (2. * rmax + skin > cell)
+            return failv(err, GDEM_ERR_ARG, "cell size smaller than the largest list cutoff 2*r_max+skin");
+        v.skin = skin;
+        v.thresh_sq = thresh * thresh;
+        v.thresh_sqf = (float)v.thresh_sq;
+        // inner rows (mixed mode): a tenth of r_max by default, never more than the skin
+        v.inner_on = 0;
+        if (T::mixed && d.inner_skin >= 0.) {
+            double si = d.inner_skin > 0. ? d.inner_skin : 0.1 * rmax;
+            if (si > skin) si = skin;
+            v.inner_on = 1;
+            v.inner_skin = si;
+            v.inner_skinf = (float)si;
+            v.inner_thresh_sqf = (float)(0.25 * si * si);
+        }
+        v.invdx = v.invdy = v.invdz = 1. / cell;
+        v.sizex = (int)ceil((v.maxx - v.minx) / cell) + 2;
+        if (v.per_x) {
+            // whole cells across the period, at least as wide as the cutoff
+            v.nxp = (int)floor(v.Lx / cell);
+            if (v.nxp < 3) return failv(err, GDEM_ERR_ARG, "periodic x: fewer than 3 cells across the period");
+            v.invdx = (double)v.nxp / v.Lx;
+            v.sizex = v.nxp + 2;
+        }
+        v.sizey = (int)ceil((v.maxy - v.miny) / cell) + 2;
+        v.sizez = (int)ceil((v.maxz - v.minz) / cell) + 2;
+        if (v.sizex > 1024 || v.sizey > 1024 || v.sizez > 1024)
+            return failv(err, GDEM_ERR_RANGE, "cell grid exceeds 1024 cells per axis (10-bit Morton keys)");
+        v.ncells = v.sizex * v.sizey * v.sizez;
+        cudaFree(cell_arena);
+        cell_arena = nullptr;
+        Arena Cc;
+        Cc.add(&v.cell_start, v.ncells);
+        Cc.add(&v.cell_end, v.ncells);
+        CKE(cudaMalloc((void**)&cell_arena, Cc.total()));
+        Cc.bind(cell_arena);
+        return GDEM_OK;
+    }
+
     int import_(const gdem_particles* p) override {
         CKE(cudaStreamSynchronize(st));
         destroy_graphs();
@@ -471,46 +517,7 @@ struct Impl : EngineBase {
                 }
             }
         }
-        // ---- grid (initialize_BoundingBox, BoundingBox.cu:370-396)
-        const double cell = d.cell_size > 0 ? d.cell_size : rmax * 4.;
-        const double skin = d.skin > 0 ? d.skin : rmax;
-        const double thresh = d.refresh_thresh > 0 ? d.refresh_thresh : (d.skin > 0 ? skin * 0.5 : rmax * 0.5);
-        if (2. * rmax + skin > cell)
-            return failv(err, GDEM_ERR_ARG, "cell size smaller than the largest list cutoff 2*r_max+skin");
-        v.skin = skin;
-        v.thresh_sq = thresh * thresh;
-        v.thresh_sqf = (float)v.thresh_sq;
-        // inner rows (mixed mode): a tenth of r_max by default, never more than the skin
-        v.inner_on = 0;
-        if (T::mixed && d.inner_skin >= 0.) {
-            double si = d.inner_skin > 0. ? d.inner_skin : 0.1 * rmax;
-            if (si > skin) si = skin;
-            v.inner_on = 1;
-            v.inner_skin = si;
-            v.inner_skinf = (float)si;
-            v.inner_thresh_sqf = (float)(0.25 * si * si);
-        }
-        v.invdx = v.invdy = v.invdz = 1. / cell;
-        v.sizex = (int)ceil((v.maxx - v.minx) / cell) + 2;
-        if (v.per_x) {
-            // whole cells across the period, at least as wide as the cutoff
-            v.nxp = (int)floor(v.Lx / cell);
-            if (v.nxp < 3) return failv(err, GDEM_ERR_ARG, "periodic x: fewer than 3 cells across the period");
-            v.invdx = (double)v.nxp / v.Lx;
-            v.sizex = v.nxp + 2;
-        }
-        v.sizey = (int)ceil((v.maxy - v.miny) / cell) + 2;
-        v.sizez = (int)ceil((v.maxz - v.minz) / cell) + 2;
-        if (v.sizex > 1024 || v.sizey > 1024 || v.sizez > 1024)
-            return failv(err, GDEM_ERR_RANGE, "cell grid exceeds 1024 cells per axis (10-bit Morton keys)");
-        v.ncells = v.sizex * v.sizey * v.sizez;
-        cudaFree(cell_arena);
-        cell_arena = nullptr;
-        Arena Cc;
-        Cc.add(&v.cell_start, v.ncells);
-        Cc.add(&v.cell_end, v.ncells);
-        CKE(cudaMalloc((void**)&cell_arena, Cc.total()));
-        Cc.bind(cell_arena);
+        if (int rc = setup_grid(rmax)) return rc;
         std::vector<float4> posh, posl;
         if (T::mixed) {
             posh.resize(n);
@@ -1028,6 +1035,33 @@ struct Impl : EngineBase {
         }
         if (!e.empty()) return failv(err, GDEM_ERR_ARG, e);
         return GDEM_OK;
+    }
+
+    // ---------------------------------------------------------------- device init
+    int init_particles(const gdem_inlet* in) override {
+        double* buf = nullptr;
+        CKE(cudaMalloc((void**)&buf, sizeof(double) * 10 * (size_t)n));
+        double *dx = buf, *dv = buf + 3 * (size_t)n, *dr = buf + 6 * (size_t)n, *dm = buf + 7 * (size_t)n,
+               *dk = buf + 8 * (size_t)n, *de = buf + 9 * (size_t)n;
+        std::string msg;
+        int rc = init_particles_device(*in, n, dx, dv, dr, dm, dk, de, st, msg);
+        std::vector<double> h((size_t)10 * n);
+        if (rc == GDEM_OK && cudaMemcpy(h.data(), buf, sizeof(double) * h.size(), cudaMemcpyDeviceToHost) != cudaSuccess) {
+            rc = GDEM_ERR_CUDA;
+            msg = "init: copy of the particles failed";
+        }
+        cudaFree(buf);
+        if (rc) return failv(err, rc, msg);
+        gdem_particles pp;
+        memset(&pp, 0, sizeof(pp));
+        pp.n = n;
+        pp.x = h.data();
+        pp.v = h.data() + 3 * (size_t)n;
+        pp.r = h.data() + 6 * (size_t)n;
+        pp.m = h.data() + 7 * (size_t)n;
+        pp.k = h.data() + 8 * (size_t)n;
+        pp.etaconst = h.data() + 9 * (size_t)n;
+        return import_(&pp);
     }
 
     // ---------------------------------------------------------------- snapshot
@@ -1661,6 +1695,23 @@ int gdem_frame_write_async(gdem_handle* h, const char* dir, int step, double len
     if (!h || !dir) return fail(h, GDEM_ERR_ARG, "frame_write_async: null");
     if (!h->eng->imported) return fail(h, GDEM_ERR_STATE, "frame before import");
     return pass(h, h->eng->frame_async(dir, step, length_factor));
+}
+
+int gdem_init_particles(gdem_handle* h, const gdem_inlet* in) {
+    if (!h || !in) return fail(h, GDEM_ERR_ARG, "init_particles: null");
+    if (in->placement != GDEM_PLACE_RANDOM && in->placement != GDEM_PLACE_LATTICE)
+        return fail(h, GDEM_ERR_ARG, "init_particles: unknown placement");
+    if (in->radius_dist < GDEM_RADIUS_MONO || in->radius_dist > GDEM_RADIUS_BIDISPERSE)
+        return fail(h, GDEM_ERR_ARG, "init_particles: unknown radius distribution");
+    if (!(in->r_a > 0) || (in->radius_dist != GDEM_RADIUS_MONO && !(in->r_b > 0)) ||
+        (in->radius_dist == GDEM_RADIUS_LOGNORMAL && !(in->r_c > 0 && in->r_d >= in->r_c)) ||
+        !(in->density > 0) || !(in->restitution > 0 && in->restitution <= 1) || !(in->youngs_modulus > 0))
+        return fail(h, GDEM_ERR_ARG, "init_particles: bad radius, density or material");
+    for (int a = 0; a < 3; a++)
+        if (!(in->box_max[a] > in->box_min[a])) return fail(h, GDEM_ERR_ARG, "init_particles: empty region");
+    const int rc = pass(h, h->eng->init_particles(in));
+    if (rc == GDEM_OK) h->eng->imported = true;
+    return rc;
 }
 
 int gdem_frames_flush(gdem_handle* h) {

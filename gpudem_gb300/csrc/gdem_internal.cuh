@@ -21,6 +21,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
+struct gdem_inlet;
+
 namespace gdem {
 
 constexpr int kBlock = 256;
@@ -548,6 +552,9 @@ int rs_blocks_for(int n);
 void launch_dist_triangle(const TriRec* tri, const double* pos, const double* r, const int* t, int m,
                           double* out4, int* hit, cudaStream_t st);
 void launch_trif(const TriRec* tri, TriRecF* out, TriLoF* lo, int ntri, cudaStream_t st);
+// device-side particle initialisation (gdem_init.cu)
+int init_particles_device(const gdem_inlet& in, int n, double* x, double* v, double* r, double* m, double* k,
+                          double* eta, cudaStream_t st, std::string& msg);
 // output frames (gdem_output.cu): write_frame_bin's payload built on the device
 size_t frame_scratch_bytes(int n);
 size_t frame_bytes(int n);

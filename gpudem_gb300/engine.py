@@ -51,7 +51,8 @@ class Engine:
     def __init__(self, scene: Scene, precision="fp64", model="linear", reorder=True,
                  store_forces=False, nei_capacity=64, wall_capacity=32, hist_capacity=32,
                  hist_wall_capacity=16, steps_per_graph=8, cell_size=-1.0, skin=None,
-                 refresh=None, box=None, bvh_every_step=False, mixed_kernel=0, occupancy=0, inner_skin=0.0):
+                 refresh=None, box=None, bvh_every_step=False, mixed_kernel=0, occupancy=0, inner_skin=0.0,
+                 import_scene=True):
         self.L = _lib.load()
         self.scene = scene
         self.n = scene.n
@@ -97,9 +98,10 @@ class Engine:
         self.ntri = 0
         if scene.tris is not None and len(scene.tris):
             self.set_mesh(scene.tris)
-        self.import_particles(scene, history=scene.history, hist_stride=scene.hist_stride)
-        if scene.mu_p is not None:
-            self.set_particle_materials(scene.mu_p, scene.e_p)
+        if import_scene:
+            self.import_particles(scene, history=scene.history, hist_stride=scene.hist_stride)
+            if scene.mu_p is not None:
+                self.set_particle_materials(scene.mu_p, scene.e_p)
 
     # ------------------------------------------------------------------ setup
     def _check(self, rc, what):
@@ -178,9 +180,12 @@ class Engine:
         n = self.n
         out = {k: np.zeros(3 * n) for k in ("x", "v", "angv")}
         out["isActive"] = np.zeros(n, np.int32)
+        for k in ("r", "m", "k", "etaconst"):
+            out[k] = np.zeros(n)
         p = _lib.Particles()
         p.n = n
         p.x, p.v, p.angv = _ptr(out["x"]), _ptr(out["v"]), _ptr(out["angv"])
+        p.r, p.m, p.k, p.etaconst = _ptr(out["r"]), _ptr(out["m"]), _ptr(out["k"]), _ptr(out["etaconst"])
         p.isActive = _ptr(out["isActive"], C.c_int)
         forces = self.store_forces if forces is None else forces
         if forces:
@@ -265,6 +270,33 @@ class Engine:
         s = C.c_void_p()
         self._check(self.L.gdem_get_stream(self.h, C.byref(s)), "gdem_get_stream")
         return int(s.value or 0)
+
+    def init_particles(self, box_min, box_max, placement="random", radius=("mono", 1e-3), density=2500.0,
+                       youngs_modulus=5e6, restitution=0.5, velocity=(0.0, 0.0, 0.0), velocity_sigma=0.0,
+                       gap=0.1, seed=1):
+        """Place and import the engine's particles on the device (the
+        reference's shuffle inlet with polydisperse radii; gdem_init_particles).
+        `radius`: ("mono", r), ("uniform", lo, hi), ("lognormal", median,
+        sigma, lo, hi) or ("bidisperse", r1, r2, fraction of r1)."""
+        inl = _lib.Inlet()
+        for a in range(3):
+            inl.box_min[a] = float(box_min[a])
+            inl.box_max[a] = float(box_max[a])
+            inl.velocity[a] = float(velocity[a])
+        inl.placement = _lib.PLACE[placement]
+        inl.radius_dist = _lib.RADIUS[radius[0]]
+        vals = [float(x) for x in radius[1:]] + [0.0] * 4
+        if radius[0] == "bidisperse":
+            inl.r_a, inl.r_b, inl.r_c = vals[0], vals[1], vals[2]
+        else:
+            inl.r_a, inl.r_b, inl.r_c, inl.r_d = vals[:4]
+        inl.density = float(density)
+        inl.youngs_modulus = float(youngs_modulus)
+        inl.restitution = float(restitution)
+        inl.velocity_sigma = float(velocity_sigma)
+        inl.gap = float(gap)
+        inl.seed = int(seed)
+        self._check(self.L.gdem_init_particles(self.h, C.byref(inl)), "gdem_init_particles")
 
     def frame_write_async(self, directory, step, length_factor=1.0):
         """Queue write_frame_bin's file <directory>/result_%012d.bin of the

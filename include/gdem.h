@@ -210,6 +210,33 @@ int gdem_export_particles(gdem_handle* h, gdem_particles* p);
  * copied with one transfer. */
 int gdem_export_positions(gdem_handle* h, double* x);
 
+/* ---- particle initialisation on the device ---- */
+enum { GDEM_PLACE_RANDOM = 0, GDEM_PLACE_LATTICE = 1 };
+enum { GDEM_RADIUS_MONO = 0, GDEM_RADIUS_UNIFORM = 1, GDEM_RADIUS_LOGNORMAL = 2, GDEM_RADIUS_BIDISPERSE = 3 };
+/* The reference's "shuffle" inlet (initializeParticles, ParticleSystem.cu:189-340;
+ * demSettings.json "inlet"), with polydisperse radii. */
+typedef struct gdem_inlet {
+    double box_min[3], box_max[3]; /* region of the particle centres (the "shuffle" box) */
+    int placement;                 /* GDEM_PLACE_RANDOM: uniform random centres, no two closer than
+                                      2 r_max (the reference's rejection sampling, done in parallel);
+                                      GDEM_PLACE_LATTICE: jittered cubic sites in random order */
+    int radius_dist;               /* GDEM_RADIUS_* */
+    double r_a, r_b, r_c, r_d;     /* MONO: r_a.  UNIFORM: [r_a, r_b].  LOGNORMAL: median r_a, sigma of
+                                      ln r r_b, clipped to [r_c, r_d].  BIDISPERSE: r_a with probability
+                                      r_c, else r_b */
+    double density;                /* mass = density * 3.14 * r^3 * 4/3 (main.cu:67) */
+    double youngs_modulus;         /* linear law: k = 4/3 (E/2) sqrt(r/2) sqrt(0.05 r) (ParticleSystem.cu:202) */
+    double restitution;            /* linear law: etaconst (ParticleSystem.cu:301) */
+    double velocity[3];            /* initial velocity: mean ... */
+    double velocity_sigma;         /* ... and Gaussian spread per component */
+    double gap;                    /* LATTICE: spacing 2 r_max (1 + gap), jitter +-gap r_max / 2 */
+    unsigned long long seed;
+} gdem_inlet;
+/* Place the engine's n_particles particles on the device and import them (as
+ * gdem_import_particles would, with no contact history).  GDEM_ERR_RANGE when
+ * the region cannot hold them. */
+int gdem_init_particles(gdem_handle* h, const gdem_inlet* inlet);
+
 /* ---- output frames and snapshots ---- */
 /* Queue the current state's output frame, the file write_frame_bin writes
  * (solver_output.cu:259-316, main.cu:276-286): <dir>/result_%012d.bin with the
