@@ -60,7 +60,10 @@ def candidate_stages(scene, precision: str):
     if precision == "mixed":
         stages.append([dict(mixed_kernel=k, occupancy=o) for k, o in KERNELS])
     skins = [f * rmax for f in SKIN_FACTORS]
-    stages.append([dict(skin=s, cell_size=max(4.0 * rmax, 2.0 * rmax + s)) for s in skins])
+    # FP64 keeps the reference's cell of at least 4 r_max (its keys and order);
+    # mixed mode takes the smallest cell the scan allows
+    cell = (lambda s: 2.0 * rmax + s) if precision == "mixed" else (lambda s: max(4.0 * rmax, 2.0 * rmax + s))
+    stages.append([dict(skin=s, cell_size=cell(s)) for s in skins])
     if precision == "mixed":
         stages.append([dict(inner_skin=f * rmax) for f in INNER_FACTORS])
     stages.append([dict(steps_per_graph=k) for k in GRAPH_STEPS])

@@ -415,8 +415,12 @@ struct Impl : EngineBase {
     // Grid, skins and refresh thresholds from the largest radius
     // (initialize_BoundingBox, BoundingBox.cu:370-396).
     int setup_grid(double rmax) {
-        const double cell = d.cell_size > 0 ? d.cell_size : rmax * 4.;
         const double skin = d.skin > 0 ? d.skin : rmax;
+        // FP64 mode keeps the reference's cell (4 r_max) for its bit-exact
+        // keys, order and cell lists; mixed mode takes the smallest cell the
+        // 27-cell scan allows, the list cutoff 2 r_max + skin, which scans
+        // (4 / 3)^3 = 2.4 times fewer candidates at the default skin
+        const double cell = d.cell_size > 0 ? d.cell_size : (T::mixed ? 2. * rmax + skin : rmax * 4.);
         const double thresh = d.refresh_thresh > 0 ? d.refresh_thresh : (d.skin > 0 ? skin * 0.5 : rmax * 0.5);
         if (2. * rmax + skin > cell)
             return failv(err, GDEM_ERR_ARG, "cell size smaller than the largest list cutoff 2*r_max+skin");

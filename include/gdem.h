@@ -70,7 +70,8 @@ typedef struct gdem_desc {
     double g[3];            /* gravity (ParticleSysShared::g) */
     double box_min[3];      /* BoundingBox min/max (BoundingBox.cu:448-478) */
     double box_max[3];
-    double cell_size;       /* <= 0: 4 * r_max (BoundingBox.cu:381) */
+    double cell_size;       /* <= 0: 4 * r_max (BoundingBox.cu:381) in FP64 mode; the list cutoff
+                               2 r_max + skin in mixed mode */
     double skin;            /* <= 0: r_max (BoundingBox.cu:386) */
     double refresh_thresh;  /* <= 0: skin / 2 (BoundingBox.cu:387) */
     /* Hertz-Mindlin material (model == GDEM_HERTZ_MINDLIN) */
