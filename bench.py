@@ -338,20 +338,24 @@ def position_error(sc, kw, steps):
 
 def run_e2e(args, sc, kw):
     """Same metric through the C ABI with host buffers: the state uploaded from
-    host memory, K steps, positions read back into pinned host memory every
-    step (write_frame_bin's frame), all inside the timed region."""
+    host memory, K steps, every step's positions read back into pinned host
+    memory (write_frame_bin's frame), all inside the timed region.  Each
+    step's copy runs on the engine's copy stream while the next step computes
+    (gdem_export_positions_async into two pinned buffers in turn); the last
+    synchronise waits for all of them."""
     import torch
     from gpudem_gb300 import engine
     n = sc.n
     steps = max(1, min(args.steps, args.e2e_steps))
     E = engine.Engine(sc, precision=args.precision, **kw)
-    frame = torch.empty(3 * n, dtype=torch.float64).pin_memory().numpy()
+    frames = [torch.empty(3 * n, dtype=torch.float64).pin_memory().numpy() for _ in range(2)]
+    frame = frames[0]
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     E.import_particles(sc, history=sc.history, hist_stride=sc.hist_stride)
-    for _ in range(steps):
+    for k in range(steps):
         E.step(1)
-        E.export_positions(out=frame)
+        E.export_positions_async(frames[k % 2])
     E.sync()
     dt_s = time.perf_counter() - t0
     E.close()
@@ -508,7 +512,7 @@ def main():
     ap.add_argument("--skin", type=float, default=-1.0)
     ap.add_argument("--v-sigma", type=float, default=0.5)
     ap.add_argument("--profile-iters", type=int, default=10)
-    ap.add_argument("--e2e-steps", type=int, default=500)
+    ap.add_argument("--e2e-steps", type=int, default=2000)
     ap.add_argument("--workload", default="poured", choices=["poured", "lattice", "batched", "channel"])
     ap.add_argument("--n-scenes", type=int, default=256)
     ap.add_argument("--seq-steps", type=int, default=200)

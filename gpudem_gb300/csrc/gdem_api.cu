@@ -96,6 +96,8 @@ struct EngineBase {
     virtual void set_mesh(const MeshData& m) = 0;
     virtual unsigned error_word() = 0;
     virtual int frame_async(const char* dir, int step, double length_factor) = 0;
+    virtual int export_positions_async(double* x) = 0;
+    virtual int sync_copies() = 0;
     virtual int frames_flush() = 0;
     virtual int save_snapshot(const char* path) = 0;
     virtual int init_particles(const gdem_inlet* in) = 0;
@@ -135,6 +137,13 @@ struct Impl : EngineBase {
 
     ~Impl() override {
         frames_shutdown();
+        if (copy_st) cudaStreamSynchronize(copy_st);
+        for (int k = 0; k < 2; k++) {
+            cudaFree(pgather[k]);
+            if (pready[k]) cudaEventDestroy(pready[k]);
+            if (pcopied[k]) cudaEventDestroy(pcopied[k]);
+        }
+        if (copy_st) cudaStreamDestroy(copy_st);
         if (st) cudaStreamSynchronize(st);
         destroy_graphs();
         cudaFree(arena);
@@ -746,6 +755,41 @@ struct Impl : EngineBase {
         return GDEM_OK;
     }
 
+    // Positions in pId order into host memory without waiting: the gather
+    // runs on the engine's stream, the copy on the copy stream after it, so
+    // the steps launched next overlap the transfer.  Two device buffers take
+    // turns; a buffer is gathered into again only after its last copy ended.
+    double* pgather[2] = {nullptr, nullptr};
+    cudaEvent_t pready[2] = {nullptr, nullptr}, pcopied[2] = {nullptr, nullptr};
+    int pslot = 0;
+
+    int export_positions_async(double* x) override {
+        if (!pgather[0]) {
+            if (!copy_st) CKE(cudaStreamCreateWithFlags(&copy_st, cudaStreamNonBlocking));
+            for (int k = 0; k < 2; k++) {
+                CKE(cudaMalloc((void**)&pgather[k], sizeof(double) * 3 * (size_t)n));
+                CKE(cudaEventCreateWithFlags(&pready[k], cudaEventDisableTiming));
+                CKE(cudaEventCreateWithFlags(&pcopied[k], cudaEventDisableTiming));
+                CKE(cudaEventRecord(pcopied[k], copy_st));
+            }
+        }
+        const int k = pslot;
+        pslot ^= 1;
+        CKE(cudaStreamWaitEvent(st, pcopied[k], 0));
+        launch_gather_positions(v, pgather[k], st);
+        CKE(cudaGetLastError());
+        CKE(cudaEventRecord(pready[k], st));
+        CKE(cudaStreamWaitEvent(copy_st, pready[k], 0));
+        CKE(cudaMemcpyAsync(x, pgather[k], sizeof(double) * 3 * (size_t)n, cudaMemcpyDeviceToHost, copy_st));
+        CKE(cudaEventRecord(pcopied[k], copy_st));
+        return GDEM_OK;
+    }
+
+    int sync_copies() override {
+        if (copy_st) CKE(cudaStreamSynchronize(copy_st));
+        return GDEM_OK;
+    }
+
     int lists(int stride, int* numNei, int* neiList, int* numNeiWall, int* neiListWall) override {
         Ctl c;
         std::vector<int> pid;
@@ -920,7 +964,7 @@ struct Impl : EngineBase {
     int frames_init() {
         if (fscratch) return GDEM_OK;
         CKE(cudaMalloc(&fscratch, frame_scratch_bytes(n)));
-        CKE(cudaStreamCreateWithFlags(&copy_st, cudaStreamNonBlocking));
+        if (!copy_st) CKE(cudaStreamCreateWithFlags(&copy_st, cudaStreamNonBlocking));
         const size_t fb = frame_bytes(n);
         for (auto& s : fslot) {
             CKE(cudaMalloc((void**)&s.dev, fb));
@@ -984,7 +1028,6 @@ struct Impl : EngineBase {
         }
         cudaFree(fscratch);
         fscratch = nullptr;
-        if (copy_st) cudaStreamDestroy(copy_st);
     }
 
     int frame_async(const char* dir, int step, double lf) override {
@@ -1681,9 +1724,16 @@ int gdem_step(gdem_handle* h, int nsteps) {
     return pass(h, h->eng->step(nsteps));
 }
 
+int gdem_export_positions_async(gdem_handle* h, double* x) {
+    if (!h || !x) return fail(h, GDEM_ERR_ARG, "export_positions_async: null");
+    if (!h->eng->imported) return fail(h, GDEM_ERR_STATE, "export before import");
+    return pass(h, h->eng->export_positions_async(x));
+}
+
 int gdem_synchronize(gdem_handle* h) {
     if (!h) return GDEM_ERR_ARG;
     CK(cudaStreamSynchronize(h->eng->st));
+    if (int rc = pass(h, h->eng->sync_copies())) return rc;
     CK(cudaGetLastError());
     if (h->eng->error_word()) return fail(h, GDEM_ERR_DEVICE, "device error word set");
     return GDEM_OK;

@@ -214,6 +214,12 @@ class Engine:
         self._check(self.L.gdem_export_positions(self.h, _vp(x)), "gdem_export_positions")
         return x
 
+    def export_positions_async(self, out):
+        """Positions in pId order into `out` (a pinned float64 array of 3n)
+        without waiting; `out` is valid after sync()."""
+        assert out.dtype == np.float64 and out.size == 3 * self.n and out.flags.c_contiguous
+        self._check(self.L.gdem_export_positions_async(self.h, _vp(out)), "gdem_export_positions_async")
+
     def lists(self, stride=MAX_NEI):
         n = self.n
         nn = np.zeros(n, np.int32)

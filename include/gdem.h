@@ -211,6 +211,11 @@ int gdem_export_particles(gdem_handle* h, gdem_particles* p);
  * copied with one transfer. */
 int gdem_export_positions(gdem_handle* h, double* x);
 
+/* gdem_export_positions without waiting: the copy into x (pinned host memory
+ * for a true overlap) runs on a copy stream while later steps compute; x is
+ * valid after gdem_synchronize.  Two copies may be in flight. */
+int gdem_export_positions_async(gdem_handle* h, double* x);
+
 /* ---- particle initialisation on the device ---- */
 enum { GDEM_PLACE_RANDOM = 0, GDEM_PLACE_LATTICE = 1 };
 enum { GDEM_RADIUS_MONO = 0, GDEM_RADIUS_UNIFORM = 1, GDEM_RADIUS_LOGNORMAL = 2, GDEM_RADIUS_BIDISPERSE = 3 };

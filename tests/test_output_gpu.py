@@ -121,3 +121,24 @@ def test_snapshot_refuses_another_engine(tmp_path):
     E = engine.Engine(sc, precision="fp64", model="hertz_mindlin")
     with pytest.raises(_lib.GdemError, match="precision"):
         E.load_snapshot(path)
+
+
+def test_async_position_exports_hold_their_steps():
+    """gdem_export_positions_async: each copy holds the positions of the step
+    it was queued after, though later steps ran meanwhile."""
+    import torch
+    from gpudem_gb300 import engine
+    sc = scene_with_inactive()
+    A = engine.Engine(sc, precision="mixed", model="hertz_mindlin")
+    B = engine.Engine(sc, precision="mixed", model="hertz_mindlin")
+    bufs = [torch.empty(3 * sc.n, dtype=torch.float64).pin_memory().numpy() for _ in range(3)]
+    want = []
+    for k in range(3):
+        A.step(40)
+        A.export_positions_async(bufs[k % 2] if k < 2 else bufs[2])
+        B.step(40)
+        want.append(B.export_positions())
+    A.step(40)
+    A.sync()
+    for k in range(3):
+        assert np.array_equal(bufs[k % 2] if k < 2 else bufs[2], want[k]), k
