@@ -781,7 +781,7 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned by
 // copies while the warp works on the current one.  Warps never wait for each
 // other.  Every mbarrier wait gives up after kSpinLimit tries and sets
 // GDEM_EW_TIMEOUT.
-constexpr int kNeiStageRows = 2;
+constexpr int kNeiStageRows = 1;
 
 struct __align__(16) WStage {
     float4 posh[32], posl[32], vel[32], rot[32], vell[32], rotl[32], refh[32];
@@ -902,9 +902,9 @@ __global__ void __launch_bounds__(kBlock, 2) k_step_mixed_wtma(View<Mixed> v, cu
 // flight together instead of one contact after another.  Shared memory per
 // warp is kept small (two stage buffers and the queue) so that many warps
 // share an SM.
-constexpr int kHidStageRows = 8;
+constexpr int kHidStageRows = 7;
 constexpr int kCoopWarps = 4;
-constexpr int kCoopQ = 3;
+constexpr int kCoopQ = 2;
 
 struct __align__(16) CStage {
     float4 posh[32], posl[32], vel[32], rot[32];
