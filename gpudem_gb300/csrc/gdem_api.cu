@@ -438,11 +438,13 @@ struct Impl : EngineBase {
         v.thresh_sqf = (float)v.thresh_sq;
         // inner rows (mixed mode): a tenth of r_max by default, never more than the skin
         v.inner_on = 0;
+        v.row_mask = 0xFFFFFFFFu;
         if (T::mixed && d.inner_skin >= 0.) {
             double si = d.inner_skin > 0. ? d.inner_skin : 0.1 * rmax;
             if (si > skin) si = skin;
             v.inner_on = 1;
             v.inner_skin = si;
+            if (n < (1 << kHintShift)) v.row_mask = (1u << kHintShift) - 1u;
             v.inner_skinf = (float)si;
             v.inner_thresh_sqf = (float)(0.25 * si * si);
         }

@@ -30,6 +30,7 @@ namespace gdem {
 constexpr int kBlock = 256;
 constexpr unsigned kNoKey = 0xFFFFFFFFu;  // sort key of inactive particles (sorted last)
 constexpr int kBvhStack = 64;
+constexpr int kHintShift = 26;   // inner-row entries: index bits below, slot hint above
 
 // ---------------------------------------------------------------- precision traits
 struct FP64 {
@@ -184,6 +185,11 @@ struct View {
     int inner_on;
     double inner_skin;
     float inner_skinf, inner_thresh_sqf;
+    // inner rows with slot hints: an entry is the partner's storage index in
+    // its low kHintShift bits and, above them, 1 + the partner's history slot
+    // as last seen (0: not known); row_mask keeps the index (all ones when
+    // entries carry no hints)
+    unsigned row_mask;
     // per-step force/torque output
     double *fx, *fy, *fz, *tx, *ty, *tz;
     double* ftmp;                    // [6 * n] scratch for reordering the force outputs

@@ -652,7 +652,20 @@ __global__ void __launch_bounds__(kBlock) k_inner(View<T> v) {
                     const float dx = image_dxf(v, hi.x - hj.x), dy = hi.y - hj.y, dz = hi.z - hj.z;
                     const float R = hi.w + hj.w + cut;
                     if (dx * dx + dy * dy + dz * dz < R * R * 1.0000039f) {
-                        if (m < v.nei_cap) v.inn[(size_t)m * n + i] = j;
+                        if (m < v.nei_cap) {
+                            // the partner's history slot, if it has one, as a hint
+                            int e = j;
+                            if (v.row_mask != 0xFFFFFFFFu) {
+                                const PBank<T> P = v.P[ctl->p];
+                                const int nc = P.nc[i];
+                                for (int q = 0; q < nc && q < 63; q++)
+                                    if (P.hid[(size_t)q * n + i] == j) {
+                                        e = j | ((q + 1) << kHintShift);
+                                        break;
+                                    }
+                            }
+                            v.inn[(size_t)m * n + i] = e;
+                        }
                         m++;
                     }
                 }

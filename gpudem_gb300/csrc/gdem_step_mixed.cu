@@ -655,7 +655,8 @@ __device__ __forceinline__ void step_one(const View<Mixed>& v, const SBank<Mixed
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             const int k = k0 + q;
-            jj[q] = k < nn ? (k < nei_s_rows ? nei_s[k * 32] : __ldg(&nei[(size_t)k * n + i])) : -1;
+            jj[q] = k < nn ? (int)((unsigned)(k < nei_s_rows ? nei_s[k * 32] : __ldg(&nei[(size_t)k * n + i])) & v.row_mask)
+                           : -1;
         }
         float4 hj[4];
 #pragma unroll
@@ -672,7 +673,7 @@ __device__ __forceinline__ void step_one(const View<Mixed>& v, const SBank<Mixed
             const int q = __ffs(hit) - 1;
             hit &= hit - 1u;
             const int k = k0 + q;
-            const int j = k < nei_s_rows ? nei_s[k * 32] : __ldg(&nei[(size_t)k * n + i]);
+            const int j = (int)((unsigned)(k < nei_s_rows ? nei_s[k * 32] : __ldg(&nei[(size_t)k * n + i])) & v.row_mask);
             const float4 hjq = __ldg(&Aposh[j]), ljq = __ldg(&Aposl[j]);
             bool fresh;
             const int slot = find_slot<T>(P.hid, n, i, nc, j, v.hist_cap, fresh);
@@ -999,6 +1000,7 @@ __global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<
     const int nsub = (n + 31) / 32;
     const int nei_rows = (n % 4 == 0) ? min(kNeiStageRows, v.nei_cap) : 0;
     const int hid_rows = (n % 4 == 0) ? min(kHidStageRows, v.hist_cap) : 0;
+    const unsigned rmask = v.row_mask;
     const PerX per = per_of<PER>(v);
     unsigned votes = 0u;
     unsigned err = 0u;
@@ -1067,7 +1069,8 @@ __global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<
 #pragma unroll
                 for (int q = 0; q < 4; q++) {
                     const int k = k0 + q;
-                    jj[q] = k < nn ? (k < nei_rows ? nei_s[k * 32] : __ldg(&nei[(size_t)k * n + i])) : -1;
+                    jj[q] = k < nn ? (int)((unsigned)(k < nei_rows ? nei_s[k * 32] : __ldg(&nei[(size_t)k * n + i])) & rmask)
+                                   : -1;
                 }
                 float4 hj[4];
 #pragma unroll
@@ -1100,12 +1103,21 @@ __global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<
                     k = 64 + __ffsll((long long)hit_hi) - 1;
                     hit_hi &= hit_hi - 1ull;
                 }
-                const int j = k < nei_rows ? nei_s[k * 32] : __ldg(&nei[(size_t)k * n + i]);
-                bool fresh;
-                const int slot = find_slot_staged(hid_s, hid_rows, P.hid, n, i, nc, j, v.hist_cap, fresh);
-                if (slot < 0) {
-                    err |= 0x4u;
-                    continue;
+                const unsigned e = (unsigned)(k < nei_rows ? nei_s[k * 32] : __ldg(&nei[(size_t)k * n + i]));
+                const int j = (int)(e & rmask);
+                // the slot hint of the inner row, checked against the key
+                const int hint = rmask != 0xFFFFFFFFu ? (int)(e >> kHintShift) - 1 : -1;
+                bool fresh = false;
+                int slot;
+                if (hint >= 0 && hint < nc && (hint < hid_rows ? hid_s[hint * 32] : P.hid[(size_t)hint * n + i]) == j) {
+                    slot = hint;
+                } else {
+                    slot = find_slot_staged(hid_s, hid_rows, P.hid, n, i, nc, j, v.hist_cap, fresh);
+                    if (slot < 0) {
+                        err |= 0x4u;
+                        continue;
+                    }
+                    if (rmask != 0xFFFFFFFFu && slot < 63) v.nei[(size_t)k * n + i] = j | ((slot + 1) << kHintShift);
                 }
                 touched |= 1ull << slot;
                 que->j[cnt][lane] = j;
