@@ -56,27 +56,26 @@ struct MeshData {
     int ntri = 0;
     char* arena = nullptr;
     TriRec* rec = nullptr;
-    BNode* nodes = nullptr;
-    BNodeF* nodesf = nullptr;  // FP32 copy of the tree (mixed-precision list build)
     double* aabb_d = nullptr;
     uint32_t* morton[2] = {nullptr, nullptr};
     int* idx[2] = {nullptr, nullptr};
     uint32_t *hist = nullptr, *tot = nullptr;  // key-sort scratch
-    char* seg = nullptr;                       // segment tree of leaf boxes
+    SegBox* seg = nullptr;                     // mesh tree boxes, level by level
+    SegBoxF* segf = nullptr;                   // their FP32 copies (mixed-precision list build)
     unsigned* done = nullptr;                  // last-CTA counter of the tree build
     double gmin[3] = {0., 0., 0.}, ginv[3] = {0., 0., 0.};
     double max_diag = 0.;                      // largest triangle bounding-box diagonal
     std::vector<double> aabb_h;
 };
 
-// Rebuild the LBVH of a mesh already set: centroid keys, their stable sort,
-// internal nodes and boxes (the set-up's own steps).
+// Rebuild the mesh tree of a mesh already set: centroid keys, their stable
+// sort, the boxes of every level (the set-up's own steps).
 static void launch_bvh_rebuild(const MeshData& M, cudaStream_t st) {
     if (M.ntri <= 0) return;
     launch_tri_keys(M.rec, M.morton[0], M.idx[0], M.ntri, M.gmin, M.ginv, st);
     radix_sort_pairs(M.morton[0], M.idx[0], M.morton[1], M.idx[1], M.hist, M.tot, M.ntri, rs_blocks_for(M.ntri), 0,
                      4, st);
-    launch_bvh_build(M.aabb_d, M.nodes, M.nodesf, M.morton[0], M.idx[0], M.seg, M.done, M.ntri, st);
+    launch_bvh_build(M.aabb_d, M.idx[0], M.seg, M.segf, M.done, M.ntri, st);
 }
 
 // Everything that depends on the precision mode.
@@ -306,9 +305,11 @@ struct Impl : EngineBase {
         mesh = &M;
         v.ntri = M.ntri;
         v.tri = M.rec;
-        v.bvh = M.nodes;
-        v.bvhf = M.nodesf;
-        v.bvh_root = 0;
+        v.seg = M.seg;
+        v.segf = M.segf;
+        v.seg_tri = M.idx[0];
+        v.seg_top = M.ntri > 0 ? seg_levels(M.ntri) - 1 : 0;
+        for (int L = 0; L < kSegMaxLevels; L++) v.seg_off[L] = L <= v.seg_top ? seg_offset_host(M.ntri, L) : 0;
         if (T::mixed) {
             cudaFree(trif);
             trif = nullptr;
@@ -363,17 +364,20 @@ struct Impl : EngineBase {
             kp.blockDim = L.block;
             kp.sharedMemBytes = (unsigned)L.smem;
             kp.kernelParams = args;
-            cudaGraphNode_t sn;
-            CKE(cudaGraphAddKernelNode(&sn, g, prev ? &prev : nullptr, prev ? 1 : 0, &kp));
+            cudaGraphNode_t sn[2];
+            int nsn = 1;
+            CKE(cudaGraphAddKernelNode(&sn[0], g, prev ? &prev : nullptr, prev ? 1 : 0, &kp));
             if (d.bvh_every_step && mesh && mesh->ntri > 0) {
+                // the mesh tree rebuild runs beside the step kernel, which
+                // reads no part of the tree; the list rebuild that reads it
+                // waits for both
                 cudaGraph_t bg;
                 CKE(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
                 launch_bvh_rebuild(*mesh, st);
                 CKE(cudaStreamEndCapture(st, &bg));
-                cudaGraphNode_t bn;
-                CKE(cudaGraphAddChildGraphNode(&bn, g, &sn, 1, bg));
+                CKE(cudaGraphAddChildGraphNode(&sn[1], g, prev ? &prev : nullptr, prev ? 1 : 0, bg));
                 cudaGraphDestroy(bg);
-                sn = bn;
+                nsn = 2;
             }
             cudaGraphNodeParams cp = {};
             cp.type = cudaGraphNodeTypeConditional;
@@ -381,7 +385,7 @@ struct Impl : EngineBase {
             cp.conditional.type = cudaGraphCondTypeIf;
             cp.conditional.size = 1;
             cudaGraphNode_t cn;
-            CKE(cudaGraphAddNode(&cn, g, &sn, nullptr, 1, &cp));
+            CKE(cudaGraphAddNode(&cn, g, sn, nullptr, nsn, &cp));
             cudaGraph_t body = cp.conditional.phGraph_out[0];
             CKE(cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0,
                                               cudaStreamCaptureModeThreadLocal));
@@ -1573,7 +1577,7 @@ int gdem_set_mesh(gdem_handle* h, const double* tris, int n_tri, const int* file
 
 // Device half of the mesh set-up, shared by gdem_set_mesh (welded here) and
 // gdem_set_mesh_indexed (welded by the caller's loader): triangle and mesh
-// AABBs, per-triangle records, centroid keys, their sort and the LBVH.  The
+// AABBs, per-triangle records, centroid keys, their sort and the mesh tree.  The
 // plane offset comes from the raw third corner (raw3) or is given (dplane).
 static int upload_mesh(gdem_handle* h, const std::vector<double>& vx, const std::vector<double>& vy,
                        const std::vector<double>& vz, const std::vector<int>& tv, const std::vector<int>& te,
@@ -1606,6 +1610,7 @@ static int upload_mesh(gdem_handle* h, const std::vector<double>& vx, const std:
         }
         if (d2 > M.max_diag * M.max_diag) M.max_diag = std::sqrt(d2);
     }
+    if (T > (1 << kSegShift)) return fail(h, GDEM_ERR_ARG, "mesh: more than 2^26 triangles");
     if (h->d.periodic_x) {
         const double L = h->d.box_max[0] - h->d.box_min[0];
         for (int t = 0; t < T; t++)
@@ -1615,20 +1620,19 @@ static int upload_mesh(gdem_handle* h, const std::vector<double>& vx, const std:
     const int SCALE = (1 << 10) - 1;
     double inv[3];
     for (int k = 0; k < 3; k++) inv[k] = SCALE / (g[3 + k] - g[k]);
-    // ---- device side: precompute records, centroid keys, sort, LBVH
+    // ---- device side: precompute records, centroid keys, sort, mesh tree
     const int NV = (int)vx.size();
     Arena A;
     double *dvx, *dvy, *dvz, *draw3;
     int *dtv, *dte;
     const int nb = rs_blocks_for(T);
     A.add(&M.rec, T);
-    A.add(&M.nodes, 2 * (size_t)T);
-    A.add(&M.nodesf, 2 * (size_t)T);
     A.add(&M.aabb_d, 6 * (size_t)T);
     A.add(&dvx, NV); A.add(&dvy, NV); A.add(&dvz, NV);
     A.add(&draw3, raw3_h ? 3 * (size_t)T : (size_t)T);
     A.add(&dtv, 3 * (size_t)T); A.add(&dte, 3 * (size_t)T);
-    A.add(&M.seg, bvh_scratch_bytes(T));
+    A.add(&M.seg, bvh_scratch_bytes(T) / sizeof(SegBox));
+    A.add(&M.segf, bvh_scratch_bytes(T) / sizeof(SegBox));
     A.add(&M.done, 1);
     A.add(&M.morton[0], T); A.add(&M.morton[1], T);
     A.add(&M.idx[0], T); A.add(&M.idx[1], T);
@@ -1656,7 +1660,7 @@ static int upload_mesh(gdem_handle* h, const std::vector<double>& vx, const std:
         M.ginv[k] = inv[k];
     }
     radix_sort_pairs(M.morton[0], M.idx[0], M.morton[1], M.idx[1], M.hist, M.tot, T, nb, 0, 4, st);
-    launch_bvh_build(M.aabb_d, M.nodes, M.nodesf, M.morton[0], M.idx[0], M.seg, M.done, T, st);
+    launch_bvh_build(M.aabb_d, M.idx[0], M.seg, M.segf, M.done, T, st);
     CK(cudaStreamSynchronize(st));
     CK(cudaGetLastError());
     h->eng->set_mesh(M);

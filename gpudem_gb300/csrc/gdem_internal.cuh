@@ -55,24 +55,20 @@ struct __align__(16) TriRec {
 };
 static_assert(sizeof(TriRec) == 256, "TriRec must be 256 bytes");
 
-// LBVH node: internal nodes [0, T-1), leaves [T-1, 2T-1).
-struct __align__(16) BNode {
+// Mesh tree: a complete binary tree over the Morton-sorted triangles, kept
+// level by level (level 0: the triangles' boxes in sorted order; node k of
+// level L: the union of nodes 2k and 2k+1 of level L-1, so it covers sorted
+// triangles [k 2^L, (k+1) 2^L)).  Every box contains the boxes below it, which
+// is all a traversal needs.
+struct __align__(16) SegBox {
     double lo[3], hi[3];
-    int left, right;   // child node indices (internal nodes)
-    int tri;           // triangle index (leaves), -1 otherwise
-    int parent;
 };
-static_assert(sizeof(BNode) == 64, "BNode must be 64 bytes");
-
-// FP32 copy of an LBVH node for the mixed-precision list build: the box
-// rounded outwards; children (internal node) or -1 - triangle index (leaf).
-struct __align__(16) BNodeF {
-    float lo[3];
-    int left;
-    float hi[3];
-    int right;
+// the same box in FP32, rounded outwards (mixed-precision list build)
+struct SegBoxF {
+    float lo[3], hi[3];
 };
-static_assert(sizeof(BNodeF) == 32, "BNodeF must be 32 bytes");
+constexpr int kSegMaxLevels = 32;
+constexpr int kSegShift = 26;   // traversal stack entries: level << kSegShift | node
 
 // Mixed-mode copy of a triangle: the first corner as a float pair, the rest
 // in FP32 (128 bytes).
@@ -209,10 +205,12 @@ struct View {
     const TriRecF* trif;             // mixed mode
     const TriLoF* trilo;             // mixed mode
     float wall_delta;                // mixed mode: bound on the FP32 error of a wall distance (m)
-    const BNode* bvh;
-    const BNodeF* bvhf;              // mixed mode: the same tree in FP32
+    const SegBox* seg;               // mesh tree boxes, level by level
+    const SegBoxF* segf;             // mixed mode: the same boxes in FP32
+    const int* seg_tri;              // triangle of each level-0 node (Morton order)
+    int seg_off[kSegMaxLevels];      // first box of each level
+    int seg_top;                     // level of the root
     int ntri;
-    int bvh_root;
     // scalars
     Material mat;
     double dt;
@@ -541,12 +539,14 @@ void launch_finalize_oob(const View<T>& v, cudaStream_t st);
 // k_tri_precompute computes them.
 void launch_tri_keys(const TriRec* rec, uint32_t* morton, int* idx, int ntri, const double* gmin,
                      const double* invrange, cudaStream_t st);
-// LBVH of the Morton-sorted triangles: leaves, a segment tree of their boxes
-// in `seg` (bvh_scratch_bytes), internal nodes with their boxes.  `done` is a
-// counter that must start at 0 (it is left at 0).  `nodesf` (may be null)
-// receives the FP32 copy of every node.
-void launch_bvh_build(const double* aabb, BNode* nodes, BNodeF* nodesf, const uint32_t* morton_sorted,
-                      const int* sorted_idx, void* seg, unsigned* done, int ntri, cudaStream_t st);
+// Mesh tree of the Morton-sorted triangles (SegBox): every level's boxes in
+// `seg` (bvh_scratch_bytes bytes) and their FP32 copies in `segf`.  `done` is
+// a counter that must start at 0 (it is left at 0).
+void launch_bvh_build(const double* aabb, const int* sorted_idx, SegBox* seg, SegBoxF* segf, unsigned* done,
+                      int ntri, cudaStream_t st);
+int seg_count_host(int n, int level);
+int seg_offset_host(int n, int level);
+int seg_levels(int n);
 size_t bvh_scratch_bytes(int ntri);
 void launch_tri_precompute(TriRec* rec, uint32_t* morton, int* idx, const double* vx,
                            const double* vy, const double* vz, const int* tv, const int* te,

@@ -1,5 +1,5 @@
 // List rebuild path of the GB300 DEM engine: Morton keys, stable LSB radix
-// sort, particle reorder, cell ranges, Verlet lists, wall LBVH and wall lists.
+// sort, particle reorder, cell ranges, Verlet lists, wall mesh tree and wall lists.
 //
 // Reference counterparts (gpudem): dk_morton_key / update_pList_withSort
 // (BoundingBox.cu:1007, :664), radixSortUint32 / CUB SortPairs
@@ -478,12 +478,22 @@ __global__ void __launch_bounds__(kBlock) k_neighbors(View<T> v, int gated) {
 }
 
 // ===================================================================== wall lists
-// LBVH traversal with an explicit stack; a triangle joins the list when its
-// AABB and its closest feature are within r + skin (BVH.cu:493-540, with
+// Mesh tree traversal with an explicit stack; a triangle joins the list when
+// its AABB and its closest feature are within r + skin (BVH.cu:493-540, with
 // sphereAABBOverlapNeighbor and dist_triangle_neighbor).  The set does not
 // depend on the tree shape: an ancestor's box contains its leaves' boxes, so
 // the box test never rejects an ancestor of a leaf that passes.  Rows are
 // sorted by triangle index, as BVH.cu:538 does.
+
+// children of mesh tree node (L, k), L > 0, pushed right first
+__device__ __forceinline__ bool seg_push(unsigned* stack, int& sp, int L, int k, int ntri) {
+    if (sp + 2 > kBvhStack) return false;
+    const int below = (ntri + (1 << (L - 1)) - 1) >> (L - 1);
+    const unsigned lv = (unsigned)(L - 1) << kSegShift;
+    if (2 * k + 1 < below) stack[sp++] = lv | (unsigned)(2 * k + 1);
+    stack[sp++] = lv | (unsigned)(2 * k);
+    return true;
+}
 template <class T, int CAP>
 __global__ void __launch_bounds__(kBlock) k_wall_lists(View<T> v, int gated) {
     Ctl* ctl = v.ctl;
@@ -508,21 +518,23 @@ __global__ void __launch_bounds__(kBlock) k_wall_lists(View<T> v, int gated) {
             const float Rsq = R * R;
             int cand[CAP];
             bool overflow = false;
-            int stack[kBvhStack];
+            unsigned stack[kBvhStack];
             const int nimg = v.per_x && (h.x + R > v.perf[1] || h.x - R < v.perf[0]) ? 2 : 1;
             for (int img = 0; img < nimg; img++) {
                 float3 ph = make_float3(h.x, h.y, h.z);
                 if (img == 1) ph.x = h.x + R > v.perf[1] ? h.x - v.Lxh : h.x + v.Lxh;
                 int sp = 0;
-                stack[sp++] = v.bvh_root;
+                stack[sp++] = (unsigned)v.seg_top << kSegShift;
                 while (sp > 0) {
-                    const BNodeF N = v.bvhf[stack[--sp]];
+                    const unsigned e = stack[--sp];
+                    const int L = (int)(e >> kSegShift), nk = (int)(e & ((1u << kSegShift) - 1u));
+                    const SegBoxF N = v.segf[v.seg_off[L] + nk];
                     const float dx = fmaxf(fmaxf(N.lo[0] - ph.x, ph.x - N.hi[0]), 0.f);
                     const float dy = fmaxf(fmaxf(N.lo[1] - ph.y, ph.y - N.hi[1]), 0.f);
                     const float dz = fmaxf(fmaxf(N.lo[2] - ph.z, ph.z - N.hi[2]), 0.f);
                     if (!(dx * dx + dy * dy + dz * dz <= Rsq)) continue;
-                    if (N.left < 0) {
-                        const int t = -1 - N.left;
+                    if (L == 0) {
+                        const int t = v.seg_tri[nk];
                         float3 qh = ph, ql = pl;
                         if (img == 1) ql.x = 0.f;  // the period's low part is within the margin
                         const FeatureF f = closest_feature_f(qh, ql, Rsq, v.trif[t]);
@@ -539,13 +551,9 @@ __global__ void __launch_bounds__(kBlock) k_wall_lists(View<T> v, int gated) {
                             cand[k] = t;
                             count++;
                         }
-                    } else {
-                        if (sp + 2 > kBvhStack) {
-                            atomicOr(&ctl->error, 0x10u);
-                            break;
-                        }
-                        stack[sp++] = N.left;
-                        stack[sp++] = N.right;
+                    } else if (!seg_push(stack, sp, L, nk, v.ntri)) {
+                        atomicOr(&ctl->error, 0x10u);
+                        break;
                     }
                 }
             }
@@ -560,7 +568,7 @@ __global__ void __launch_bounds__(kBlock) k_wall_lists(View<T> v, int gated) {
             const double Rsq = R * R;
             int cand[CAP];
             bool overflow = false;
-            int stack[kBvhStack];
+            unsigned stack[kBvhStack];
             // periodic x: a sphere within R of an x face also queries the mesh
             // at its image one period away (no triangle is found twice: the
             // mesh's triangles are narrower than a quarter period)
@@ -568,13 +576,14 @@ __global__ void __launch_bounds__(kBlock) k_wall_lists(View<T> v, int gated) {
             for (int img = 0; img < nimg; img++) {
                 const double px = img == 0 ? pi.x : (pi.x + R > v.maxx ? pi.x - v.Lx : pi.x + v.Lx);
                 int sp = 0;
-                stack[sp++] = v.bvh_root;
+                stack[sp++] = (unsigned)v.seg_top << kSegShift;
                 while (sp > 0) {
-                    const int node = stack[--sp];
-                    const BNode& B = v.bvh[node];
+                    const unsigned e = stack[--sp];
+                    const int L = (int)(e >> kSegShift), nk = (int)(e & ((1u << kSegShift) - 1u));
+                    const SegBox& B = v.seg[v.seg_off[L] + nk];
                     if (!sphere_aabb(px, py, pz, Rsq, B.lo, B.hi)) continue;
-                    if (B.tri >= 0) {
-                        const int t = B.tri;
+                    if (L == 0) {
+                        const int t = v.seg_tri[nk];
                         const Feature f = closest_feature(px, py, pz, Rsq, v.tri[t]);
                         if (f.dist < pi.w + v.skin) {
                             if (count >= CAP) {
@@ -589,13 +598,9 @@ __global__ void __launch_bounds__(kBlock) k_wall_lists(View<T> v, int gated) {
                             cand[k] = t;
                             count++;
                         }
-                    } else {
-                        if (sp + 2 > kBvhStack) {
-                            atomicOr(&ctl->error, 0x10u);
-                            break;
-                        }
-                        stack[sp++] = B.left;
-                        stack[sp++] = B.right;
+                    } else if (!seg_push(stack, sp, L, nk, v.ntri)) {
+                        atomicOr(&ctl->error, 0x10u);
+                        break;
                     }
                 }
             }
@@ -831,7 +836,7 @@ void launch_tri_precompute(TriRec* rec, uint32_t* morton, int* idx, const double
 }
 
 // Centroid keys of the triangles from their records (the key formula of
-// k_tri_precompute), for rebuilding the LBVH of a mesh already set.
+// k_tri_precompute), for rebuilding the tree of a mesh already set.
 __global__ void k_tri_keys(const TriRec* rec, uint32_t* morton, int* idx, int ntri, double gminx, double gminy,
                            double gminz, double irx, double iry, double irz) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -854,24 +859,9 @@ void launch_tri_keys(const TriRec* rec, uint32_t* morton, int* idx, int ntri, co
                                                   invrange[1], invrange[2]);
 }
 
-// ---- Karras (2012) LBVH over the Morton-sorted triangles.  Keys that tie are
-// told apart by their sorted position, so every key is distinct.
-__device__ __forceinline__ int lbvh_delta(const uint32_t* key, int n, int i, int j) {
-    if (j < 0 || j >= n) return -1;
-    const uint32_t a = key[i], b = key[j];
-    if (a == b) return 32 + __clz((unsigned)(i ^ j));
-    return __clz(a ^ b);
-}
-
-// Node boxes without a bottom-up climb: a segment tree over the sorted leaf
-// boxes (level L, node k covers sorted leaves [k 2^L, (k+1) 2^L) ∩ [0, n)),
-// built per 512 leaves in shared memory by one CTA each, the levels above by
-// the last CTA to finish (atomic counter, no waiting).  An internal node's box
-// is then the union over the O(log n) tree nodes covering its leaf range: the
-// same minima and maxima a recursive refit takes, in any order.
-struct __align__(16) SegBox {
-    double lo[3], hi[3];
-};
+// ---- mesh tree: built per 512 sorted triangles in shared memory by one CTA
+// each, the levels above by the last CTA to finish (atomic counter, no
+// waiting).
 
 __host__ __device__ __forceinline__ int seg_count(int n, int level) {
     return (int)(((long long)n + (1ll << level) - 1) >> level);
@@ -886,6 +876,8 @@ int seg_levels(int n) {
     while (seg_count(n, L) > 1) L++;
     return L + 1;
 }
+int seg_count_host(int n, int level) { return seg_count(n, level); }
+int seg_offset_host(int n, int level) { return seg_offset(n, level); }
 
 __device__ __forceinline__ SegBox seg_union(const SegBox& a, const SegBox& b) {
     SegBox c;
@@ -909,22 +901,19 @@ __device__ __forceinline__ SegBox seg_load_cg(const SegBox* p) {
 constexpr int kSegTile = 512;
 constexpr int kSegTileLevels = 10;  // levels 0..9 inside one CTA's 512 leaves
 
-// FP32 node with its box rounded outwards (nf may be null)
-__device__ __forceinline__ void put_nodef(BNodeF* nf, int i, const double* lo, const double* hi, int left,
-                                          int right) {
-    if (!nf) return;
-    BNodeF F;
+// box and its FP32 copy (rounded outwards)
+__device__ __forceinline__ void put_box(SegBox* seg, SegBoxF* segf, int i, const SegBox& b) {
+    seg[i] = b;
+    SegBoxF f;
     for (int k = 0; k < 3; k++) {
-        F.lo[k] = __double2float_rd(lo[k]);
-        F.hi[k] = __double2float_ru(hi[k]);
+        f.lo[k] = __double2float_rd(b.lo[k]);
+        f.hi[k] = __double2float_ru(b.hi[k]);
     }
-    F.left = left;
-    F.right = right;
-    nf[i] = F;
+    segf[i] = f;
 }
 
-__global__ void __launch_bounds__(kSegTile) k_lbvh_leaves(BNode* nodes, BNodeF* nf, const double* aabb,
-                                                         const int* sorted_idx, SegBox* seg, unsigned* done, int n) {
+__global__ void __launch_bounds__(kSegTile) k_mesh_tree(const double* aabb, const int* sorted_idx, SegBox* seg,
+                                                         SegBoxF* segf, unsigned* done, int n) {
     __shared__ SegBox sb[kSegTile];
     const int tid = threadIdx.x;
     const int l = blockIdx.x * kSegTile + tid;
@@ -935,16 +924,7 @@ __global__ void __launch_bounds__(kSegTile) k_lbvh_leaves(BNode* nodes, BNodeF* 
             b.lo[k] = aabb[6 * t + k];
             b.hi[k] = aabb[6 * t + 3 + k];
         }
-        BNode& L = nodes[n - 1 + l];
-        for (int k = 0; k < 3; k++) {
-            L.lo[k] = b.lo[k];
-            L.hi[k] = b.hi[k];
-        }
-        L.tri = t;
-        L.left = L.right = -1;
-        L.parent = -1;
-        put_nodef(nf, n - 1 + l, b.lo, b.hi, -1 - t, -1);
-        seg[l] = b;
+        put_box(seg, segf, l, b);
         sb[tid] = b;
     }
     __syncthreads();
@@ -963,7 +943,7 @@ __global__ void __launch_bounds__(kSegTile) k_lbvh_leaves(BNode* nodes, BNodeF* 
         __syncthreads();
         if (live) {
             sb[local] = c;
-            seg[seg_offset(n, L) + k] = c;
+            put_box(seg, segf, seg_offset(n, L) + k, c);
         }
         __syncthreads();
     }
@@ -975,78 +955,50 @@ __global__ void __launch_bounds__(kSegTile) k_lbvh_leaves(BNode* nodes, BNodeF* 
     __syncthreads();
     if (!last) return;
     __threadfence();
-    for (int L = kSegTileLevels; seg_count(n, L - 1) > 1; L++) {
+    int L = kSegTileLevels;  // the lowest level not built yet
+    // through L2 while the level below holds more boxes than one tile
+    for (; seg_count(n, L - 1) > kSegTile; L++) {
         const int cnt = seg_count(n, L), below = seg_count(n, L - 1);
         const int ob = seg_offset(n, L - 1), oc = seg_offset(n, L);
         for (int k = tid; k < cnt; k += blockDim.x) {
             SegBox c = seg_load_cg(seg + ob + 2 * k);
             if (2 * k + 1 < below) c = seg_union(c, seg_load_cg(seg + ob + 2 * k + 1));
-            seg[oc + k] = c;
+            put_box(seg, segf, oc + k, c);
         }
         __threadfence();
         __syncthreads();
     }
+    // the rest from one tile of the level below, in shared memory: node k of
+    // m levels up sits at entry k 2^m of the tile
+    const int cb = seg_count(n, L - 1);
+    if (cb > 1) {
+        if (tid < cb) sb[tid] = seg_load_cg(seg + seg_offset(n, L - 1) + tid);
+        __syncthreads();
+        for (int m = 1; (cb + (1 << (m - 1)) - 1) >> (m - 1) > 1; m++) {
+            const int span = 1 << m;
+            const int local = tid * span;
+            const bool live = local < cb;
+            SegBox c;
+            if (live) {
+                c = sb[local];
+                const int right = local + (span >> 1);
+                if (right < cb) c = seg_union(c, sb[right]);
+            }
+            __syncthreads();
+            if (live) {
+                sb[local] = c;
+                put_box(seg, segf, seg_offset(n, L - 1 + m) + tid, c);
+            }
+            __syncthreads();
+        }
+    }
     if (tid == 0) *done = 0u;
 }
 
-__global__ void k_lbvh_internal(BNode* nodes, BNodeF* nf, const uint32_t* key, const SegBox* seg, int n) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n - 1) return;
-    const int d = (lbvh_delta(key, n, i, i + 1) - lbvh_delta(key, n, i, i - 1)) >= 0 ? 1 : -1;
-    const int dmin = lbvh_delta(key, n, i, i - d);
-    int lmax = 2;
-    while (lbvh_delta(key, n, i, i + lmax * d) > dmin) lmax <<= 1;
-    int l = 0;
-    for (int t = lmax >> 1; t >= 1; t >>= 1)
-        if (lbvh_delta(key, n, i, i + (l + t) * d) > dmin) l += t;
-    const int j = i + l * d;
-    const int dnode = lbvh_delta(key, n, i, j);
-    int s = 0;
-    int t = l;
-    do {
-        t = (t + 1) >> 1;
-        if (lbvh_delta(key, n, i, i + (s + t) * d) > dnode) s += t;
-    } while (t > 1);
-    const int gamma = i + s * d + (d < 0 ? d : 0);
-    const int lo = i < j ? i : j, hi = i < j ? j : i;
-    const int left = (lo == gamma) ? (n - 1 + gamma) : gamma;
-    const int right = (hi == gamma + 1) ? (n - 1 + gamma + 1) : gamma + 1;
-    // box of the sorted leaves [lo, hi]: the segment-tree nodes that tile it
-    SegBox box;
-    for (int k = 0; k < 3; k++) {
-        box.lo[k] = 1e300;
-        box.hi[k] = -1e300;
-    }
-    int a = lo, b = hi + 1, L = 0, off = 0;
-    while (a < b) {
-        if (a & 1) box = seg_union(box, seg[off + a++]);
-        if (b & 1) box = seg_union(box, seg[off + --b]);
-        off += seg_count(n, L);
-        a >>= 1;
-        b >>= 1;
-        L++;
-    }
-    BNode& N = nodes[i];
-    for (int k = 0; k < 3; k++) {
-        N.lo[k] = box.lo[k];
-        N.hi[k] = box.hi[k];
-    }
-    N.left = left;
-    N.right = right;
-    N.tri = -1;
-    nodes[left].parent = i;
-    nodes[right].parent = i;
-    if (i == 0) N.parent = -1;
-    put_nodef(nf, i, box.lo, box.hi, left, right);
-}
-
-void launch_bvh_build(const double* aabb, BNode* nodes, BNodeF* nodesf, const uint32_t* morton_sorted,
-                      const int* sorted_idx, void* seg, unsigned* done, int ntri, cudaStream_t st) {
+void launch_bvh_build(const double* aabb, const int* sorted_idx, SegBox* seg, SegBoxF* segf, unsigned* done,
+                      int ntri, cudaStream_t st) {
     if (ntri <= 0) return;
-    SegBox* sg = static_cast<SegBox*>(seg);
-    k_lbvh_leaves<<<(ntri + kSegTile - 1) / kSegTile, kSegTile, 0, st>>>(nodes, nodesf, aabb, sorted_idx, sg, done,
-                                                                         ntri);
-    if (ntri > 1) k_lbvh_internal<<<grid_for(ntri - 1), kBlock, 0, st>>>(nodes, nodesf, morton_sorted, sg, ntri);
+    k_mesh_tree<<<(ntri + kSegTile - 1) / kSegTile, kSegTile, 0, st>>>(aabb, sorted_idx, seg, segf, done, ntri);
 }
 
 // the segment tree's nodes: every level up to the root, and at least the
