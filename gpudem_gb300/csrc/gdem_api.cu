@@ -347,7 +347,10 @@ struct Impl : EngineBase {
         CKE(cudaGraphCreate(&g, 0));
         cudaGraphNode_t prev = nullptr;
         View<T> vs = sv();
-        const StepLaunch L = step_launch(vs);
+        const bool tree_branch = d.bvh_every_step && mesh && mesh->ntri > 0;
+        // the tree rebuild's kernels get CTA slots of their own beside the
+        // persistent step kernel, instead of waiting for it to drain
+        const StepLaunch L = step_launch(vs, tree_branch ? kTreeReserve : 0);
         for (int k = 0; k < steps; k++) {
             // every handle must belong to a conditional node: the inner-rows
             // handle exists only with inner rows (else the kernel gets hnd twice
@@ -367,7 +370,7 @@ struct Impl : EngineBase {
             cudaGraphNode_t sn[2];
             int nsn = 1;
             CKE(cudaGraphAddKernelNode(&sn[0], g, prev ? &prev : nullptr, prev ? 1 : 0, &kp));
-            if (d.bvh_every_step && mesh && mesh->ntri > 0) {
+            if (tree_branch) {
                 // the mesh tree rebuild runs beside the step kernel, which
                 // reads no part of the tree; the list rebuild that reads it
                 // waits for both

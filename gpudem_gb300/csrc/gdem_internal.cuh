@@ -584,8 +584,13 @@ struct StepLaunch {
     dim3 grid, block;
     size_t smem;
 };
-StepLaunch step_launch(const View<FP64>& v);
-StepLaunch step_launch(const View<Mixed>& v);
+// `reserve`: resident CTA slots the persistent step kernel leaves free for a
+// graph branch that runs beside it (the mesh tree rebuild); the FP64 kernel
+// is not persistent and ignores it.
+StepLaunch step_launch(const View<FP64>& v, int reserve = 0);
+StepLaunch step_launch(const View<Mixed>& v, int reserve = 0);
+// CTA slots left free beside the per-step mesh tree rebuild
+constexpr int kTreeReserve = 4;
 // stats and probes (gdem_stats.cu)
 template <class T>
 void launch_stats(const View<T>& v, double* partials, int nblk, cudaStream_t st);

@@ -9,7 +9,7 @@ void launch_step(const View<FP64>& v, cudaStream_t st, cudaGraphConditionalHandl
     launch_step_any<FP64>(v, st, cond, use_cond);
 }
 
-StepLaunch step_launch(const View<FP64>& v) {
+StepLaunch step_launch(const View<FP64>& v, int) {
     return StepLaunch{step_kernel_any<FP64>(v), dim3((v.n + kBlock - 1) / kBlock), dim3(kBlock), 0};
 }
 

@@ -1285,7 +1285,7 @@ int sm_count() {
 }
 }  // namespace
 
-StepLaunch step_launch(const View<Mixed>& v) {
+StepLaunch step_launch(const View<Mixed>& v, int reserve) {
     const int ntiles = (v.n + kBlock - 1) / kBlock;
     const int kind = kernel_kind(v);
     if (kind == 0) {
@@ -1299,7 +1299,11 @@ StepLaunch step_launch(const View<Mixed>& v) {
         if (per_sm < 1) per_sm = 1;
         const int nsub = (v.n + 31) / 32;
         const int need = (nsub + kCoopWarps - 1) / kCoopWarps;
-        const int grid = need < per_sm * sm_count() ? need : per_sm * sm_count();
+        // GDEM_COOP_RESERVE overrides a nonzero reserve (tuning)
+        static const int env_reserve = env_int("GDEM_COOP_RESERVE", -1);
+        const int res = reserve > 0 && env_reserve >= 0 ? env_reserve : reserve;
+        const int full = per_sm * sm_count() - res > 1 ? per_sm * sm_count() - res : 1;
+        const int grid = need < full ? need : full;
         return StepLaunch{fn, dim3(grid), dim3(kCoopWarps * 32), smem};
     }
     if (kind == 1) {
