@@ -498,14 +498,15 @@ def run_batched(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--steps", type=int, default=None, help="timed steps (2000; 500 for the channel)")
     ap.add_argument("--warmup", type=int, default=40)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--n", type=int, default=None, help="spheres (1M; 10M for the channel)")
     ap.add_argument("--ntri", type=int, default=None, help="triangles (50k; 200k for the channel)")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--model", default="hertz_mindlin", choices=["linear", "hertz_mindlin"])
-    ap.add_argument("--error-steps", type=int, default=1000)
+    ap.add_argument("--error-steps", type=int, default=None,
+                    help="steps of the mixed-vs-FP64 position comparison (1000; 500 for the channel)")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--traffic", type=float, default=None,
@@ -521,13 +522,23 @@ def main():
     ap.add_argument("--autotune", action="store_true",
                     help="batched workload: tune kernel, occupancy, skin, cell size and graph length first")
     ap.add_argument("--bvh-once", action="store_true",
-                    help="build the static mesh's tree once instead of in every step")
+                    help="build the static mesh's tree once instead of in every step (the channel's default)")
+    ap.add_argument("--tree-every-step", action="store_true",
+                    help="channel: rebuild the static mesh's tree in every step, as the chute workload does")
     ap.add_argument("--settle-steps", type=int, default=12000)
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     channel = args.workload == "channel"
+    # the channel runs 500 steps over a static mesh whose tree is built once;
+    # the chute bed 2,000 steps with the tree rebuilt in every step
+    if args.steps is None:
+        args.steps = 500 if channel else 2000
+    if args.error_steps is None:
+        args.error_steps = 500 if channel else 1000
+    if channel and not args.tree_every_step:
+        args.bvh_once = True
     if args.n is None:
         args.n = 10_000_000 if channel else 1_000_000
     if args.ntri is None:

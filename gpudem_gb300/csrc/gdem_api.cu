@@ -52,6 +52,27 @@ struct Arena {
     }
 };
 
+// f(lo, hi) over [0, n) in contiguous chunks, one host thread each (one
+// thread for small n); f must not throw.
+template <class F>
+static void host_parallel_for(int n, F f) {
+    unsigned nt = std::thread::hardware_concurrency();
+    nt = nt == 0 ? 1u : (nt > 32u ? 32u : nt);
+    if (n < (1 << 16)) nt = 1;
+    if (nt == 1) {
+        f(0, n);
+        return;
+    }
+    const int chunk = (int)((n + nt - 1) / nt);
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < nt; t++) {
+        const int lo = (int)t * chunk, hi = lo + chunk < n ? lo + chunk : n;
+        if (lo >= hi) break;
+        th.emplace_back(f, lo, hi);
+    }
+    for (auto& x : th) x.join();
+}
+
 struct MeshData {
     int ntri = 0;
     char* arena = nullptr;
@@ -484,106 +505,132 @@ struct Impl : EngineBase {
         destroy_graphs();
         v.per_particle_mat = 0;
         const int H = v.hist_cap, HW = v.histw_cap;
-        std::vector<double4_32a> pos(n);
-        std::vector<V4> vel(n), rot(n), mat(n);
+        const bool hist = p->numCont && p->indHis && p->hist_stride > 0;
+        const bool histw = p->numContWall && p->indHisWall && p->hist_stride > 0;
         std::vector<int> pid(n), nc(n, 0), ncw(n, 0);
-        std::vector<int> hid((size_t)n * H, -1), hwid((size_t)n * HW, -1);
-        std::vector<R> hx((size_t)n * H, 0), hy((size_t)n * H, 0), hz((size_t)n * H, 0);
-        std::vector<R> hwx((size_t)n * HW, 0), hwy((size_t)n * HW, 0), hwz((size_t)n * HW, 0);
+        // history lengths, capacity checks, the slot rows in use, r_max
+        int qmax = 0, qwmax = 0;
         double rmax = 0.;
         for (int i = 0; i < n; i++) {
-            const double r = p->r[i];
-            pos[i] = make_double4_32a(wrap_x(p->x[3 * i]), p->x[3 * i + 1], p->x[3 * i + 2], r);
-            // derived per-particle constants in the operation order of
-            // ParticleSystem.cu:294-333 (rsq = r*r, sqrtm, invm, moi = 2/5 m rsq)
-            const double rsq = r * r;
-            const double sqrtm = sqrt(p->m[i]);
-            const double invm = 1. / p->m[i];
-            const double moi = 2. / 5. * p->m[i] * rsq;
-            const double invmoi = 1. / moi;
-            vel[i].x = p->v ? (R)p->v[3 * i] : R(0);
-            vel[i].y = p->v ? (R)p->v[3 * i + 1] : R(0);
-            vel[i].z = p->v ? (R)p->v[3 * i + 2] : R(0);
-            vel[i].w = (R)invm;
-            rot[i].x = p->angv ? (R)p->angv[3 * i] : R(0);
-            rot[i].y = p->angv ? (R)p->angv[3 * i + 1] : R(0);
-            rot[i].z = p->angv ? (R)p->angv[3 * i + 2] : R(0);
-            rot[i].w = (R)((p->isActive && p->isActive[i] != 1) ? 0 : 1);
-            mat[i].x = (R)p->k[i];
-            mat[i].y = (R)p->etaconst[i];
-            mat[i].z = (R)sqrtm;
-            mat[i].w = (R)invmoi;
-            pid[i] = i;
-            if (rmax < r) rmax = r;
-            if (p->numCont && p->indHis && p->hist_stride > 0) {
+            if (rmax < p->r[i]) rmax = p->r[i];
+            if (hist) {
                 nc[i] = p->numCont[i];
                 if (nc[i] > H) return failv(err, GDEM_ERR_CAPACITY, "import: history longer than hist_capacity");
-                for (int q = 0; q < nc[i]; q++) {
-                    const size_t src = (size_t)i * p->hist_stride + q, dst = (size_t)q * n + i;
-                    hid[dst] = p->indHis[src];
-                    hx[dst] = (R)p->deltHisx[src];
-                    hy[dst] = (R)p->deltHisy[src];
-                    hz[dst] = (R)p->deltHisz[src];
-                }
+                if (nc[i] > qmax) qmax = nc[i];
             }
-            if (p->numContWall && p->indHisWall && p->hist_stride > 0) {
+            if (histw) {
                 ncw[i] = p->numContWall[i];
                 if (ncw[i] > HW)
                     return failv(err, GDEM_ERR_CAPACITY, "import: wall history longer than hist_wall_capacity");
-                for (int q = 0; q < ncw[i]; q++) {
+                if (ncw[i] > qwmax) qwmax = ncw[i];
+            }
+        }
+        std::vector<double4_32a> pos(n);
+        std::vector<V4> vel(n), rot(n), mat(n);
+        std::vector<float4> posh(T::mixed ? n : 0), posl(T::mixed ? n : 0), vl(T::mixed ? n : 0),
+            wl(T::mixed ? n : 0);
+        // only the slot rows some particle uses travel; the device clears the rest
+        std::vector<int> hid((size_t)n * qmax), hwid((size_t)n * qwmax);
+        std::vector<R> hx((size_t)n * qmax), hy((size_t)n * qmax), hz((size_t)n * qmax);
+        std::vector<R> hwx((size_t)n * qwmax), hwy((size_t)n * qwmax), hwz((size_t)n * qwmax);
+        host_parallel_for(n, [&](int lo, int hi) {
+            for (int i = lo; i < hi; i++) {
+                const double r = p->r[i];
+                pos[i] = make_double4_32a(wrap_x(p->x[3 * i]), p->x[3 * i + 1], p->x[3 * i + 2], r);
+                // derived per-particle constants in the operation order of
+                // ParticleSystem.cu:294-333 (rsq = r*r, sqrtm, invm, moi = 2/5 m rsq)
+                const double rsq = r * r;
+                const double sqrtm = sqrt(p->m[i]);
+                const double invm = 1. / p->m[i];
+                const double moi = 2. / 5. * p->m[i] * rsq;
+                const double invmoi = 1. / moi;
+                vel[i].x = p->v ? (R)p->v[3 * i] : R(0);
+                vel[i].y = p->v ? (R)p->v[3 * i + 1] : R(0);
+                vel[i].z = p->v ? (R)p->v[3 * i + 2] : R(0);
+                vel[i].w = (R)invm;
+                rot[i].x = p->angv ? (R)p->angv[3 * i] : R(0);
+                rot[i].y = p->angv ? (R)p->angv[3 * i + 1] : R(0);
+                rot[i].z = p->angv ? (R)p->angv[3 * i + 2] : R(0);
+                rot[i].w = (R)((p->isActive && p->isActive[i] != 1) ? 0 : 1);
+                mat[i].x = (R)p->k[i];
+                mat[i].y = (R)p->etaconst[i];
+                mat[i].z = (R)sqrtm;
+                mat[i].w = (R)invmoi;
+                pid[i] = i;
+                if (T::mixed) {
+                    // float pairs: the FP32 rounding and what it left out
+                    const double xs[3] = {pos[i].x, pos[i].y, pos[i].z};
+                    float hh[3], ll[3];
+                    for (int k = 0; k < 3; k++) {
+                        hh[k] = (float)xs[k];
+                        ll[k] = (float)(xs[k] - (double)hh[k]);
+                    }
+                    const float rh = (float)pos[i].w, rl = (float)(pos[i].w - (double)rh);
+                    posh[i] = make_float4(hh[0], hh[1], hh[2], rot[i].w == R(1) ? rh : -rh);
+                    posl[i] = make_float4(ll[0], ll[1], ll[2], rl);
+                    const double vv[3] = {p->v ? p->v[3 * i] : 0., p->v ? p->v[3 * i + 1] : 0.,
+                                          p->v ? p->v[3 * i + 2] : 0.};
+                    const double ww[3] = {p->angv ? p->angv[3 * i] : 0., p->angv ? p->angv[3 * i + 1] : 0.,
+                                          p->angv ? p->angv[3 * i + 2] : 0.};
+                    vl[i] = make_float4((float)(vv[0] - (double)vel[i].x), (float)(vv[1] - (double)vel[i].y),
+                                        (float)(vv[2] - (double)vel[i].z), 0.f);
+                    wl[i] = make_float4((float)(ww[0] - (double)rot[i].x), (float)(ww[1] - (double)rot[i].y),
+                                        (float)(ww[2] - (double)rot[i].z), 0.f);
+                }
+            }
+            // slot rows (slot q of particle i at q * n + i), row by row
+            for (int q = 0; q < qmax; q++)
+                for (int i = lo; i < hi; i++) {
                     const size_t src = (size_t)i * p->hist_stride + q, dst = (size_t)q * n + i;
-                    hwid[dst] = p->indHisWall[src];
-                    hwx[dst] = (R)p->deltHisxWall[src];
-                    hwy[dst] = (R)p->deltHisyWall[src];
-                    hwz[dst] = (R)p->deltHiszWall[src];
+                    const bool on = q < nc[i];
+                    hid[dst] = on ? p->indHis[src] : -1;
+                    hx[dst] = on ? (R)p->deltHisx[src] : R(0);
+                    hy[dst] = on ? (R)p->deltHisy[src] : R(0);
+                    hz[dst] = on ? (R)p->deltHisz[src] : R(0);
                 }
-            }
-        }
+            for (int q = 0; q < qwmax; q++)
+                for (int i = lo; i < hi; i++) {
+                    const size_t src = (size_t)i * p->hist_stride + q, dst = (size_t)q * n + i;
+                    const bool on = q < ncw[i];
+                    hwid[dst] = on ? p->indHisWall[src] : -1;
+                    hwx[dst] = on ? (R)p->deltHisxWall[src] : R(0);
+                    hwy[dst] = on ? (R)p->deltHisyWall[src] : R(0);
+                    hwz[dst] = on ? (R)p->deltHiszWall[src] : R(0);
+                }
+        });
         if (int rc = setup_grid(rmax)) return rc;
-        std::vector<float4> posh, posl;
-        if (T::mixed) {
-            posh.resize(n);
-            posl.resize(n);
-            for (int i = 0; i < n; i++) {
-                const double xs[3] = {pos[i].x, pos[i].y, pos[i].z};
-                float hh[3], ll[3];
-                for (int k = 0; k < 3; k++) {
-                    hh[k] = (float)xs[k];
-                    ll[k] = (float)(xs[k] - (double)hh[k]);
-                }
-                const float rh = (float)pos[i].w, rl = (float)(pos[i].w - (double)rh);
-                posh[i] = make_float4(hh[0], hh[1], hh[2], rot[i].w == R(1) ? rh : -rh);
-                posl[i] = make_float4(ll[0], ll[1], ll[2], rl);
-            }
-        }
         const SBank<T>& S = v.S[0];
         const PBank<T>& P = v.P[0];
-#define UP(dst, src, cnt) CKE(cudaMemcpyAsync(dst, src.data(), sizeof(src[0]) * (cnt), cudaMemcpyHostToDevice, st))
+#define UP(dst, src, cnt) \
+    if ((cnt) > 0) CKE(cudaMemcpyAsync(dst, src.data(), sizeof(src[0]) * (cnt), cudaMemcpyHostToDevice, st))
         if (!T::mixed) UP(S.pos, pos, n);
         UP(S.vel, vel, n); UP(S.rot, rot, n);
         if (T::mixed) {
             UP(S.posh, posh, n);
             UP(S.posl, posl, n);
-            std::vector<float4> vl(n), wl(n);
-            for (int i = 0; i < n; i++) {
-                // low parts of the velocity / spin pairs: input minus its FP32 rounding
-                const double vv[3] = {p->v ? p->v[3 * i] : 0., p->v ? p->v[3 * i + 1] : 0., p->v ? p->v[3 * i + 2] : 0.};
-                const double ww[3] = {p->angv ? p->angv[3 * i] : 0., p->angv ? p->angv[3 * i + 1] : 0.,
-                                      p->angv ? p->angv[3 * i + 2] : 0.};
-                vl[i] = make_float4((float)(vv[0] - (double)vel[i].x), (float)(vv[1] - (double)vel[i].y),
-                                    (float)(vv[2] - (double)vel[i].z), 0.f);
-                wl[i] = make_float4((float)(ww[0] - (double)rot[i].x), (float)(ww[1] - (double)rot[i].y),
-                                    (float)(ww[2] - (double)rot[i].z), 0.f);
-            }
             UP(S.vell, vl, n);
             UP(S.rotl, wl, n);
         }
         UP(P.mat, mat, n); UP(P.pid, pid, n);
-        UP(P.nc, nc, n); UP(P.hid, hid, (size_t)n * H);
-        UP(P.hx, hx, (size_t)n * H); UP(P.hy, hy, (size_t)n * H); UP(P.hz, hz, (size_t)n * H);
-        UP(P.ncw, ncw, n); UP(P.hwid, hwid, (size_t)n * HW);
-        UP(P.hwx, hwx, (size_t)n * HW); UP(P.hwy, hwy, (size_t)n * HW); UP(P.hwz, hwz, (size_t)n * HW);
+        UP(P.nc, nc, n); UP(P.hid, hid, (size_t)n * qmax);
+        UP(P.hx, hx, (size_t)n * qmax); UP(P.hy, hy, (size_t)n * qmax); UP(P.hz, hz, (size_t)n * qmax);
+        UP(P.ncw, ncw, n); UP(P.hwid, hwid, (size_t)n * qwmax);
+        UP(P.hwx, hwx, (size_t)n * qwmax); UP(P.hwy, hwy, (size_t)n * qwmax); UP(P.hwz, hwz, (size_t)n * qwmax);
 #undef UP
+        // the slot rows no particle uses: no key (-1), zero springs
+        const size_t r0 = (size_t)n * qmax, r1 = (size_t)n * H, w0 = (size_t)n * qwmax, w1 = (size_t)n * HW;
+        if (r1 > r0) {
+            CKE(cudaMemsetAsync(P.hid + r0, 0xFF, sizeof(int) * (r1 - r0), st));
+            CKE(cudaMemsetAsync(P.hx + r0, 0, sizeof(R) * (r1 - r0), st));
+            CKE(cudaMemsetAsync(P.hy + r0, 0, sizeof(R) * (r1 - r0), st));
+            CKE(cudaMemsetAsync(P.hz + r0, 0, sizeof(R) * (r1 - r0), st));
+        }
+        if (w1 > w0) {
+            CKE(cudaMemsetAsync(P.hwid + w0, 0xFF, sizeof(int) * (w1 - w0), st));
+            CKE(cudaMemsetAsync(P.hwx + w0, 0, sizeof(R) * (w1 - w0), st));
+            CKE(cudaMemsetAsync(P.hwy + w0, 0, sizeof(R) * (w1 - w0), st));
+            CKE(cudaMemsetAsync(P.hwz + w0, 0, sizeof(R) * (w1 - w0), st));
+        }
         if (T::mixed) {
             CKE(cudaMemsetAsync(P.cx, 0, sizeof(R) * (size_t)n * H, st));
             CKE(cudaMemsetAsync(P.cy, 0, sizeof(R) * (size_t)n * H, st));

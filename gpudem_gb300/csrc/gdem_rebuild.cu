@@ -859,7 +859,7 @@ void launch_tri_keys(const TriRec* rec, uint32_t* morton, int* idx, int ntri, co
                                                   invrange[1], invrange[2]);
 }
 
-// ---- mesh tree: built per 512 sorted triangles in shared memory by one CTA
+// ---- mesh tree: built per 256 sorted triangles in shared memory by one CTA
 // each, the levels above by the last CTA to finish (atomic counter, no
 // waiting).
 
@@ -898,8 +898,8 @@ __device__ __forceinline__ SegBox seg_load_cg(const SegBox* p) {
     return b;
 }
 
-constexpr int kSegTile = 512;
-constexpr int kSegTileLevels = 10;  // levels 0..9 inside one CTA's 512 leaves
+constexpr int kSegTile = 256;
+constexpr int kSegTileLevels = 9;  // levels 0..8 inside one CTA's 256 leaves
 
 // box and its FP32 copy (rounded outwards)
 __device__ __forceinline__ void put_box(SegBox* seg, SegBoxF* segf, int i, const SegBox& b) {
@@ -928,7 +928,7 @@ __global__ void __launch_bounds__(kSegTile) k_mesh_tree(const double* aabb, cons
         sb[tid] = b;
     }
     __syncthreads();
-    // levels 1..10 of this CTA's leaves
+    // levels 1..8 of this CTA's leaves
     for (int L = 1; L < kSegTileLevels; L++) {
         const int span = 1 << L;
         const int local = tid * span;             // first leaf (CTA-relative) of node tid at level L

@@ -1,4 +1,4 @@
-"""Wall lists from the mesh tree on a mesh of more than 512 x 512 triangles,
+"""Wall lists from the mesh tree on a mesh of more than 256 x 256 triangles,
 where the tree's upper levels are built through L2 before the last tile is
 reduced in shared memory (k_mesh_tree), checked against a brute-force scan:
 every triangle whose AABB comes within r + skin of the sphere, kept when the
@@ -47,7 +47,7 @@ def _brute_rows(E, sc, x, skin):
 def test_wall_lists_large_mesh(precision):
     from gpudem_gb300 import engine
     sc = _floor_scene()
-    assert sc.tris.shape[0] > 512 * 512 * 2
+    assert sc.tris.shape[0] > 256 * 256 * 2
     E = engine.Engine(sc, precision=precision, box=(np.array([-0.55, -0.05, -0.15]), np.array([0.55, 0.05, 0.15])),
                       wall_capacity=48)
     skin = float(sc.r.max())
