@@ -491,7 +491,8 @@ def run_batched(args):
                       "autotune_s": None if tuned is None else round(tune_s, 1),
                       "one_by_one_value": seq_value, "one_by_one_steps_per_scene": seq_steps,
                       "batched_over_one_by_one": value / seq_value, "rebuilds_in_timed_region": reb},
-           "clocks": clk.summary(), "gpu_launches": args.steps + reb * 19}
+           "clocks": clk.summary(),
+           "gpu_launches": args.steps + reb * 19 + int(st1["inner_builds"] - st0["inner_builds"])}
     print(json.dumps(out))
 
 
