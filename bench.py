@@ -36,7 +36,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "particle-steps/s at 1M spheres, FP32-mixed vs FP64 plain on 1 GB300 (err≤1e-4·r_min)"
-TRAFFIC_POURED_BED_1M = 740_104_704.0   # bytes per step-kernel launch, ncu on the default workload
+TRAFFIC_POURED_BED_1M = 739_527_424.0   # bytes per step-kernel launch, ncu on the default workload
 # bytes per sphere of one step-kernel launch on the periodic channel, from an
 # ncu capture of the 1M-sphere channel (the 10M one is too large to capture);
 # the launch's traffic scales with the spheres it steps
