@@ -496,7 +496,8 @@ def run_batched(args):
     print(json.dumps(out))
 
 
-def main():
+def parse_args(argv=None):
+    """Command line with the workload-dependent defaults filled in."""
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=None, help="timed steps (2000; 500 for the channel)")
@@ -529,7 +530,7 @@ def main():
     ap.add_argument("--settle-steps", type=int, default=12000)
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu", action="store_true")
-    args = ap.parse_args()
+    args = ap.parse_args(argv)
     args.warmup = max(3, args.warmup)
     channel = args.workload == "channel"
     # the channel runs 500 steps over a static mesh whose tree is built once;
@@ -544,6 +545,11 @@ def main():
         args.n = 10_000_000 if channel else 1_000_000
     if args.ntri is None:
         args.ntri = 200_000 if channel else 50_000
+    return args
+
+
+def main():
+    args = parse_args()
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "batched":
