@@ -28,6 +28,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -225,8 +226,7 @@ def run_engine(args):
     stream = torch.cuda.ExternalStream(E.stream())
     if dist:
         dist.barrier()
-    out_dir = os.path.join(ROOT, "gpurun_out") if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp"
-    clk = Clocks(os.path.join(out_dir, f"clocks_r{rank}.csv"))
+    clk = Clocks(os.path.join(args.clocks_dir or tempfile.gettempdir(), f"clocks_r{rank}.csv"))
     ms, st0, st1 = _time_steps(E, args.steps, args.warmup, stream, clk)
     ms, value = aggregate_replicas(ms, 0.5 * (st0["n_active"] + st1["n_active"]), args.steps, dist)
     # dominant kernel: the step kernel alone, CUDA events on the engine stream
@@ -457,8 +457,7 @@ def run_batched(args):
         tune_s = time.time() - t0
     E = engine.Engine(packed, precision=args.precision, **kw)
     stream = torch.cuda.ExternalStream(E.stream())
-    out_dir = os.path.join(ROOT, "gpurun_out") if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp"
-    clk = Clocks(os.path.join(out_dir, "clocks_batched.csv"))
+    clk = Clocks(os.path.join(args.clocks_dir or tempfile.gettempdir(), "clocks_batched.csv"))
     ms, st0, st1 = _time_steps(E, args.steps, args.warmup, stream, clk)
     n_act = 0.5 * (st0["n_active"] + st1["n_active"])
     value = n_act * args.steps / (ms / 1e3)
@@ -530,6 +529,8 @@ def parse_args(argv=None):
     ap.add_argument("--settle-steps", type=int, default=12000)
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--clocks-dir", default=None,
+                    help="where the nvidia-smi clock samples of the timed region go (default: the temp dir)")
     args = ap.parse_args(argv)
     args.warmup = max(3, args.warmup)
     channel = args.workload == "channel"
