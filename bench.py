@@ -475,7 +475,7 @@ def run_batched(args):
         seq_ps += 0.5 * (a0["n_active"] + a1["n_active"]) * seq_steps
         Es.close()
     seq_value = seq_ps / (seq_ms / 1e3)
-    out = {"metric": "particle-steps/s, 256 uneven scenes in one launch (batched) vs one by one",
+    out = {"metric": f"particle-steps/s, {len(scs)} uneven scenes in one launch (batched) vs one by one",
            "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": "f32" if args.precision == "mixed" else "f64",
