@@ -103,6 +103,13 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(rows)}
 
 
+def sort_launches(n_keys):
+    """Kernels of one 4-pass radix sort of n_keys keys: upsweep and scatter per
+    pass, plus a digit-scan kernel per pass above 32 tiles of 2048 keys."""
+    tiles = max(1, -(-n_keys // 2048))
+    return 4 * (2 if tiles <= 32 else 3)
+
+
 def algorithmic_bytes(st, n_active, s=8, s_h=8):
     """Force-kernel bytes per launch: N(S_read+S_write) + 4(2N + sum n_nei +
     sum n_w) + (sum n_c + sum n_wc)(6 s_h + 8), S_read = 24 + 8s, S_write = 24 + 6s.
@@ -297,12 +304,13 @@ def run_engine(args):
                    "wall_contacts_per_sphere": round(stk["n_wall_contacts"] / max(stk["n_active"], 1), 3),
                    **extra},
         "clocks": clk.summary(),
-        # one step kernel per step (+ the mesh tree rebuild: keys, 4 x 3 sort
-        # passes, tree) + the kernels of each list rebuild (keys, 4 x 3 sort
-        # passes, reorder (+ its inverse order in mixed mode), cell clear, cell
-        # ranges, Verlet (+ the FP32 position copy in FP64 mode), walls) + each
+        # one step kernel per step (+ the mesh tree rebuild: keys, 4 sort
+        # passes, tree) + the kernels of each list rebuild (keys, 4 sort passes,
+        # reorder (+ its inverse order in mixed mode), cell clear, cell ranges,
+        # Verlet (+ the FP32 position copy in FP64 mode), walls) + each
         # inner-row build
-        "gpu_launches": args.steps * (1 + (0 if args.bvh_once else 14)) + reb * 19
+        "gpu_launches": args.steps * (1 + (0 if args.bvh_once else 2 + sort_launches(int(sc.tris.shape[0]))))
+                        + reb * (7 + sort_launches(sc.n))
                         + int(st1["inner_builds"] - st0["inner_builds"]),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
@@ -491,7 +499,8 @@ def run_batched(args):
                       "one_by_one_value": seq_value, "one_by_one_steps_per_scene": seq_steps,
                       "batched_over_one_by_one": value / seq_value, "rebuilds_in_timed_region": reb},
            "clocks": clk.summary(),
-           "gpu_launches": args.steps + reb * 19 + int(st1["inner_builds"] - st0["inner_builds"])}
+           "gpu_launches": args.steps + reb * (7 + sort_launches(packed.n))
+                           + int(st1["inner_builds"] - st0["inner_builds"])}
     print(json.dumps(out))
 
 

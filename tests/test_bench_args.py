@@ -27,3 +27,11 @@ def test_channel_defaults():
 
 def test_warmup_floor():
     assert bench.parse_args(["--warmup", "1"]).warmup == 3
+
+
+def test_sort_launch_count():
+    # up to 32 tiles of 2048 keys the digit scan folds into the scatter kernel
+    assert bench.sort_launches(50_768) == 8
+    assert bench.sort_launches(32 * 2048) == 8
+    assert bench.sort_launches(32 * 2048 + 1) == 12
+    assert bench.sort_launches(1_000_000) == 12
