@@ -23,7 +23,7 @@ EXPORTED = [
     "gdem_sort_keys_noalloc", "gdem_set_mesh_indexed", "gdem_set_particle_materials",
     "gdem_dist_triangle", "gdem_export_mesh", "gdem_get_stream", "gdem_profile_step",
     "gdem_export_positions", "gdem_frame_write_async", "gdem_frames_flush", "gdem_save_snapshot",
-    "gdem_load_snapshot", "gdem_init_particles", "gdem_export_positions_async",
+    "gdem_load_snapshot", "gdem_init_particles", "gdem_export_positions_async", "gdem_check_snapshot",
 ]
 PLACE = {"random": 0, "lattice": 1}
 RADIUS = {"mono": 0, "uniform": 1, "lognormal": 2, "bidisperse": 3}
@@ -138,6 +138,7 @@ def load(build_if_missing: bool = False):
     L.gdem_frames_flush.argtypes = [vp]
     L.gdem_save_snapshot.argtypes = [vp, C.c_char_p]
     L.gdem_load_snapshot.argtypes = [vp, C.c_char_p]
+    L.gdem_check_snapshot.argtypes = [C.c_char_p, C.c_int]
     L.gdem_init_particles.argtypes = [vp, C.POINTER(Inlet)]
     L.gdem_export_positions_async.argtypes = [vp, vp]
     for nm in EXPORTED:

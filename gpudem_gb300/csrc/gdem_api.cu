@@ -99,6 +99,70 @@ static void launch_bvh_rebuild(const MeshData& M, cudaStream_t st) {
     launch_bvh_build(M.aabb_d, M.idx[0], M.seg, M.segf, M.done, M.ntri, st);
 }
 
+// Snapshot file: this header, then per particle in pId order the state
+// arrays of the precision (mixed: posh, posl, vel, vell, rot, rotl; FP64: pos,
+// vel, rot; 16 or 32 bytes each) and the material record, then the particle
+// history (n counts, the live keys, their spring terms) and the wall history
+// in the same form.
+struct SnapHeader {
+    char magic[8];
+    int version, n, precision, model, hist_cap, histw_cap, per_particle_mat, rsize;
+    unsigned long long steps;
+    unsigned error, pad;
+};
+
+// Structure of a snapshot file, read without touching a device: the header,
+// the exact length, history counts within the stored capacities, and every
+// history key an index of this state (partner particles in [0, n), triangles
+// in [0, n_tri)).  A snapshot that fails is refused before any upload.
+static int check_snapshot_file(const char* path, int n_tri, SnapHeader* out, std::string& msg) {
+    FILE* fp = fopen(path, "rb");
+    if (!fp) {
+        msg = std::string("snapshot: cannot open ") + path;
+        return GDEM_ERR_ARG;
+    }
+    SnapHeader hd;
+    bool ok = fread(&hd, 1, sizeof(hd), fp) == sizeof(hd);
+    auto bad = [&](const char* why) {
+        fclose(fp);
+        msg = std::string("snapshot: ") + why;
+        return GDEM_ERR_ARG;
+    };
+    if (!ok || memcmp(hd.magic, "GDEMSNAP", 8) != 0 || hd.version != 1) return bad("not a snapshot file");
+    const bool mixed = hd.precision == GDEM_MIXED;
+    if (hd.n <= 0 || (hd.precision != GDEM_FP64 && !mixed) || hd.rsize != (mixed ? 4 : 8) || hd.hist_cap < 0 ||
+        hd.histw_cap < 0 || hd.hist_cap > 64 || hd.histw_cap > 64)
+        return bad("header out of range");
+    const size_t n = (size_t)hd.n;
+    const int nterms = mixed ? 6 : 3;
+    const long state = (long)(n * (mixed ? 7 * 16 : 4 * 32));
+    if (fseek(fp, state, SEEK_CUR) != 0) return bad("truncated");
+    for (int part = 0; part < 2; part++) {
+        const int cap = part == 0 ? hd.hist_cap : hd.histw_cap;
+        const long long id_end = part == 0 ? hd.n : n_tri;
+        std::vector<int> cnt(n);
+        if (fread(cnt.data(), sizeof(int), n, fp) != n) return bad("truncated");
+        size_t tot = 0;
+        for (size_t q = 0; q < n; q++) {
+            if (cnt[q] < 0 || cnt[q] > cap) return bad("a history longer than its capacity");
+            tot += (size_t)cnt[q];
+        }
+        std::vector<int> id(tot);
+        if (tot && fread(id.data(), sizeof(int), tot, fp) != tot) return bad("truncated");
+        for (size_t e = 0; e < tot; e++)
+            if (id[e] < 0 || id[e] >= id_end)
+                return bad(part == 0 ? "a history partner outside [0, n)" : "a wall history triangle outside the mesh");
+        if (fseek(fp, (long)(tot * nterms * hd.rsize), SEEK_CUR) != 0) return bad("truncated");
+    }
+    const long here = ftell(fp);
+    fseek(fp, 0, SEEK_END);
+    const long end = ftell(fp);
+    if (here != end) return bad("truncated, or trailing bytes");
+    fclose(fp);
+    if (out) *out = hd;
+    return GDEM_OK;
+}
+
 // Everything that depends on the precision mode.
 struct EngineBase {
     virtual ~EngineBase() {}
@@ -194,6 +258,10 @@ struct Impl : EngineBase {
         v.store_forces = d.store_forces ? 1 : 0;
         v.kernel_variant = d.mixed_kernel >= 0 && d.mixed_kernel <= 3 ? d.mixed_kernel : 0;
         v.occupancy = d.occupancy > 0 ? d.occupancy : 0;
+        // failure-detection tests only: fewer tries for the step kernels'
+        // pipeline waits, so that a wait gives up and reports GDEM_EW_TIMEOUT
+        v.wait_tries = kSpinLimit;
+        if (const char* wt = getenv("GDEM_TEST_WAIT_TRIES")) v.wait_tries = (unsigned)strtoul(wt, nullptr, 10);
         v.reorder = d.reorder == 0 ? 0 : 1;
         v.rs_blocks = rs_blocks_for(n);
         const size_t H = (size_t)n * v.hist_cap, HW = (size_t)n * v.histw_cap;
@@ -508,21 +576,36 @@ struct Impl : EngineBase {
         const bool hist = p->numCont && p->indHis && p->hist_stride > 0;
         const bool histw = p->numContWall && p->indHisWall && p->hist_stride > 0;
         std::vector<int> pid(n), nc(n, 0), ncw(n, 0);
-        // history lengths, capacity checks, the slot rows in use, r_max
+        // history lengths, capacity checks, the slot rows in use, r_max.  The
+        // live history keys become device indices (partner particles, mesh
+        // triangles), so each is checked here, before anything is uploaded.
+        const int ntri = mesh ? mesh->ntri : 0;
         int qmax = 0, qwmax = 0;
         double rmax = 0.;
         for (int i = 0; i < n; i++) {
             if (rmax < p->r[i]) rmax = p->r[i];
             if (hist) {
                 nc[i] = p->numCont[i];
-                if (nc[i] > H) return failv(err, GDEM_ERR_CAPACITY, "import: history longer than hist_capacity");
+                if (nc[i] < 0) return failv(err, GDEM_ERR_ARG, "import: negative numCont");
+                if (nc[i] > H || nc[i] > p->hist_stride)
+                    return failv(err, GDEM_ERR_CAPACITY, "import: history longer than hist_capacity");
                 if (nc[i] > qmax) qmax = nc[i];
+                for (int q = 0; q < nc[i]; q++) {
+                    const int j = p->indHis[(size_t)i * p->hist_stride + q];
+                    if (j < 0 || j >= n) return failv(err, GDEM_ERR_ARG, "import: history partner id outside [0, n)");
+                }
             }
             if (histw) {
                 ncw[i] = p->numContWall[i];
-                if (ncw[i] > HW)
+                if (ncw[i] < 0) return failv(err, GDEM_ERR_ARG, "import: negative numContWall");
+                if (ncw[i] > HW || ncw[i] > p->hist_stride)
                     return failv(err, GDEM_ERR_CAPACITY, "import: wall history longer than hist_wall_capacity");
                 if (ncw[i] > qwmax) qwmax = ncw[i];
+                for (int q = 0; q < ncw[i]; q++) {
+                    const int t = p->indHisWall[(size_t)i * p->hist_stride + q];
+                    if (t < 0 || t >= ntri)
+                        return failv(err, GDEM_ERR_ARG, "import: wall history triangle outside the mesh");
+                }
             }
         }
         std::vector<double4_32a> pos(n);
@@ -1175,13 +1258,6 @@ struct Impl : EngineBase {
     // and model (with its mesh set) continues the run bit for bit: storage
     // order, lists and rebuild times differ, and none of them enters the
     // results.
-    struct SnapHeader {
-        char magic[8];
-        int version, n, precision, model, hist_cap, histw_cap, per_particle_mat, rsize;
-        unsigned long long steps;
-        unsigned error, pad;
-    };
-
     int save_snapshot(const char* path) override {
         if (!path) return failv(err, GDEM_ERR_ARG, "snapshot: null path");
         Ctl c;
@@ -1275,6 +1351,10 @@ struct Impl : EngineBase {
 
     int load_snapshot(const char* path) override {
         if (!path) return failv(err, GDEM_ERR_ARG, "snapshot: null path");
+        {
+            std::string msg;
+            if (int rc = check_snapshot_file(path, mesh ? mesh->ntri : 0, nullptr, msg)) return failv(err, rc, msg);
+        }
         FILE* fp = fopen(path, "rb");
         if (!fp) return failv(err, GDEM_ERR_ARG, std::string("snapshot: cannot open ") + path);
         bool ok = true;
@@ -1311,7 +1391,11 @@ struct Impl : EngineBase {
         const int nterms = T::mixed ? 6 : 3;
         std::vector<int> nc(n), ncw(n), ids, idsw;
         std::vector<R> vals, valsw;
-        auto get_hist = [&](std::vector<int>& cnt, std::vector<int>& id, std::vector<R>& val, int cap) {
+        // every history key becomes a device index (a partner particle or a
+        // mesh triangle): a key outside [0, id_end) refuses the file before
+        // anything is uploaded
+        bool ids_ok = true;
+        auto get_hist = [&](std::vector<int>& cnt, std::vector<int>& id, std::vector<R>& val, int cap, int id_end) {
             get(cnt.data(), sizeof(int) * (size_t)n);
             size_t tot = 0;
             for (int q = 0; q < n && ok; q++) {
@@ -1323,11 +1407,15 @@ struct Impl : EngineBase {
             val.resize(tot * nterms);
             get(id.data(), sizeof(int) * tot);
             get(val.data(), sizeof(R) * val.size());
+            for (size_t e = 0; e < tot && ok; e++)
+                if (id[e] < 0 || id[e] >= id_end) ids_ok = false;
         };
-        get_hist(nc, ids, vals, H);
-        get_hist(ncw, idsw, valsw, HW);
+        get_hist(nc, ids, vals, H, n);
+        get_hist(ncw, idsw, valsw, HW, mesh ? mesh->ntri : 0);
         fclose(fp);
         if (!ok) return failv(err, GDEM_ERR_ARG, "snapshot: truncated, or a history longer than this engine's capacity");
+        if (!ids_ok)
+            return failv(err, GDEM_ERR_ARG, "snapshot: a history key outside the particles or the mesh triangles");
         // set the engine up as an import would (grid, lists), from the
         // reference-layout view of the snapshot ...
         std::vector<double> x(3 * (size_t)n), vv(3 * (size_t)n), ww(3 * (size_t)n), r(n), m(n), k(n), eta(n);
@@ -1535,9 +1623,9 @@ int gdem_set_mesh(gdem_handle* h, const double* tris, int n_tri, const int* file
     cudaStream_t st = h->eng->st;
     cudaStreamSynchronize(st);
     MeshData& M = h->mesh;
-    cudaFree(M.arena);
-    M = MeshData();
     if (n_tri == 0) {
+        cudaFree(M.arena);
+        M = MeshData();
         h->eng->set_mesh(M);
         return h->eng->imported ? pass(h, h->eng->rebuild()) : GDEM_OK;
     }
@@ -1634,6 +1722,34 @@ static int upload_mesh(gdem_handle* h, const std::vector<double>& vx, const std:
                        const double* raw3_h, const double* dplane_h, int T) {
     cudaStream_t st = h->eng->st;
     MeshData& M = h->mesh;
+    // ---- a corrupt mesh is refused before anything reaches the device:
+    // non-finite coordinates or plane offsets, and triangles of zero area
+    // (their unit normal, n = e01 x e02 / |e01 x e02|, does not exist)
+    for (size_t q = 0; q < vx.size(); q++)
+        if (!std::isfinite(vx[q]) || !std::isfinite(vy[q]) || !std::isfinite(vz[q]))
+            return fail(h, GDEM_ERR_ARG, "mesh: a vertex coordinate is NaN or infinite");
+    for (int t = 0; t < T; t++) {
+        if (raw3_h && !(std::isfinite(raw3_h[3 * t]) && std::isfinite(raw3_h[3 * t + 1]) &&
+                        std::isfinite(raw3_h[3 * t + 2])))
+            return fail(h, GDEM_ERR_ARG, "mesh: a triangle corner is NaN or infinite");
+        if (dplane_h && !std::isfinite(dplane_h[t])) return fail(h, GDEM_ERR_ARG, "mesh: a plane offset is NaN or infinite");
+        const int a = tv[3 * t], b = tv[3 * t + 1], c = tv[3 * t + 2];
+        const double e1[3] = {vx[b] - vx[a], vy[b] - vy[a], vz[b] - vz[a]};
+        const double e2[3] = {vx[c] - vx[a], vy[c] - vy[a], vz[c] - vz[a]};
+        const double cr[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2],
+                              e1[0] * e2[1] - e1[1] * e2[0]};
+        if (cr[0] == 0. && cr[1] == 0. && cr[2] == 0.)
+            return fail(h, GDEM_ERR_ARG, "mesh: a triangle has zero area (repeated or collinear corners)");
+        if (h->d.periodic_x) {
+            const double L = h->d.box_max[0] - h->d.box_min[0];
+            const double w = std::max(vx[a], std::max(vx[b], vx[c])) - std::min(vx[a], std::min(vx[b], vx[c]));
+            if (!(w < 0.25 * L)) return fail(h, GDEM_ERR_ARG, "periodic x: a triangle is wider than a quarter period");
+        }
+    }
+    if (T > (1 << kSegShift)) return fail(h, GDEM_ERR_ARG, "mesh: more than 2^26 triangles");
+    // the mesh is sound: the previous one (if any) goes
+    cudaFree(M.arena);
+    M = MeshData();
     // ---- triangle AABBs and the mesh AABB, in the loader's comparison order
     M.aabb_h.assign(6 * (size_t)T, 0.);
     double g[6] = {1e300, 1e300, 1e300, -1e300, -1e300, -1e300};
@@ -1659,13 +1775,6 @@ static int upload_mesh(gdem_handle* h, const std::vector<double>& vx, const std:
             d2 += e * e;
         }
         if (d2 > M.max_diag * M.max_diag) M.max_diag = std::sqrt(d2);
-    }
-    if (T > (1 << kSegShift)) return fail(h, GDEM_ERR_ARG, "mesh: more than 2^26 triangles");
-    if (h->d.periodic_x) {
-        const double L = h->d.box_max[0] - h->d.box_min[0];
-        for (int t = 0; t < T; t++)
-            if (!(M.aabb_h[6 * t + 3] - M.aabb_h[6 * t] < 0.25 * L))
-                return fail(h, GDEM_ERR_ARG, "periodic x: a triangle is wider than a quarter period");
     }
     const int SCALE = (1 << 10) - 1;
     double inv[3];
@@ -1726,9 +1835,9 @@ int gdem_set_mesh_indexed(gdem_handle* h, const gdem_mesh_arrays* m) {
         return fail(h, GDEM_ERR_ARG, "mesh arrays missing");
     cudaStreamSynchronize(h->eng->st);
     MeshData& M = h->mesh;
-    cudaFree(M.arena);
-    M = MeshData();
     if (T == 0) {
+        cudaFree(M.arena);
+        M = MeshData();
         h->eng->set_mesh(M);
         return h->eng->imported ? pass(h, h->eng->rebuild()) : GDEM_OK;
     }
@@ -1738,6 +1847,8 @@ int gdem_set_mesh_indexed(gdem_handle* h, const gdem_mesh_arrays* m) {
         const int a = m->tri_i0[t], b = m->tri_i1[t], c = m->tri_i2[t];
         // the loader stores each triangle's vertex ids ascending (sort3, TriangleMesh.cu:89-103)
         if (a < 0 || c >= NV || a > b || b > c) return fail(h, GDEM_ERR_ARG, "need 0 <= tri_i0 <= tri_i1 <= tri_i2 < nVert");
+        if (m->tri_e0[t] < 0 || m->tri_e1[t] < 0 || m->tri_e2[t] < 0)
+            return fail(h, GDEM_ERR_ARG, "mesh: negative edge id");
         tv[3 * t] = a; tv[3 * t + 1] = b; tv[3 * t + 2] = c;
         te[3 * t] = m->tri_e0[t]; te[3 * t + 1] = m->tri_e1[t]; te[3 * t + 2] = m->tri_e2[t];
     }
@@ -1840,6 +1951,12 @@ int gdem_load_snapshot(gdem_handle* h, const char* path) {
     const int rc = pass(h, h->eng->load_snapshot(path));
     if (rc == GDEM_OK) h->eng->imported = true;
     return rc;
+}
+
+int gdem_check_snapshot(const char* path, int n_tri) {
+    if (!path || n_tri < 0) return GDEM_ERR_ARG;
+    std::string msg;
+    return check_snapshot_file(path, n_tri, nullptr, msg);
 }
 
 int gdem_export_positions(gdem_handle* h, double* x) {

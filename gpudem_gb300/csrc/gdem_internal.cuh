@@ -91,6 +91,10 @@ struct __align__(16) TriLoF {
 };
 static_assert(sizeof(TriLoF) == 48, "TriLoF must be 48 bytes");
 
+// Tries of a bounded wait on an mbarrier (bulk-copy completion) before the
+// kernel gives up and sets GDEM_EW_TIMEOUT.
+constexpr unsigned kSpinLimit = 1u << 22;
+
 struct Ctl {
     int s;                    // state bank holding the current state
     int p;                    // property bank holding current properties/history
@@ -229,6 +233,8 @@ struct View {
     int per_particle_mat;            // Hertz-Mindlin: mu and damping from mat.x, mat.y of each particle
     int kernel_variant;              // mixed step kernel: 0 default, 1 cooperative, 2 staged, 3 one-pass
     int occupancy;                   // mixed step kernel: resident CTAs per SM to size for (0 default)
+    unsigned wait_tries;             // mixed step kernels: tries of each pipeline wait on a bulk copy
+                                     // (kSpinLimit; GDEM_TEST_WAIT_TRIES lowers it to test the timeout path)
     // the scalars above rounded to FP32 once, for the mixed step
     float dtf, gxf, gyf, gzf, thresh_sqf;
     float muf, kn_cf, sn_cf, kt_cf, damp_cf, mu_rollf;

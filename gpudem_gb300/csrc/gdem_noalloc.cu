@@ -19,8 +19,11 @@
 // memory, so it exists as soon as the module is loaded on a device.  The first
 // call on each device looks its address up with cudaGetSymbolAddress (which
 // loads the module there if it is not loaded yet) and keeps it for later
-// calls.  Make that first call on each device before any stream capture
-// begins.
+// calls, together with the id of the context it belongs to.  Make that first
+// call on each device before any stream capture begins.  A context torn down
+// and made again (cudaDeviceReset, then any CUDA call) loads the module anew,
+// possibly at another address: the next call sees the new context id and
+// looks the address up again, so that call too belongs before any capture.
 //
 // Nothing in the scratch must start at zero: every pass overwrites the whole
 // histogram it reads (one count per digit and tile) and every position of the
@@ -32,6 +35,7 @@
 // overlap on the GPU: two calls in flight at once (on different streams, or
 // from different host threads without ordering) race on the scratch and give
 // wrong results.  Order them on one stream or with events.
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -58,15 +62,48 @@ static __device__ __align__(256) unsigned char g_sort_scratch[kScratchBytes];
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 unsigned char* g_scratch_ptr[kMaxDevices] = {};
+unsigned long long g_scratch_ctx[kMaxDevices] = {};
 
-// Address of this device's scratch, looked up on the first call per device.
+// Id of the current context (unique for the life of the process, unlike its
+// handle), through the driver entry points the runtime hands out, so the
+// library needs no link against the driver library.
+cudaError_t current_context_id(unsigned long long* id) {
+    using GetCurrent = CUresult (*)(CUcontext*);
+    using GetId = CUresult (*)(CUcontext, unsigned long long*);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    if (!get_current || !get_id) {
+        void* a = nullptr;
+        void* b = nullptr;
+        cudaDriverEntryPointQueryResult qa, qb;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa) != cudaSuccess ||
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb) != cudaSuccess ||
+            qa != cudaDriverEntryPointSuccess || qb != cudaDriverEntryPointSuccess)
+            return cudaErrorNotSupported;
+        get_current = reinterpret_cast<GetCurrent>(a);
+        get_id = reinterpret_cast<GetId>(b);
+    }
+    CUcontext ctx = nullptr;
+    if (get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, id) != CUDA_SUCCESS) return cudaErrorContextIsDestroyed;
+    return cudaSuccess;
+}
+
+// Address of this device's scratch in the current context: looked up on the
+// first call per device and again whenever the context has changed (or no
+// context is current on this thread yet: the lookup makes the device's
+// primary context current).
 cudaError_t scratch_for(int dev, unsigned char** out) {
     std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_scratch_ptr[dev]) {
+    unsigned long long ctx = 0;
+    const bool known = current_context_id(&ctx) == cudaSuccess;
+    if (!known || !g_scratch_ptr[dev] || g_scratch_ctx[dev] != ctx) {
         void* p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_sort_scratch);
         if (e != cudaSuccess) return e;
+        const cudaError_t ce = current_context_id(&ctx);
+        if (ce != cudaSuccess) return ce;
         g_scratch_ptr[dev] = static_cast<unsigned char*>(p);
+        g_scratch_ctx[dev] = ctx;
     }
     *out = g_scratch_ptr[dev];
     return cudaSuccess;

@@ -737,9 +737,11 @@ __global__ void __launch_bounds__(kBlock, MINB) k_step_mixed(View<Mixed> v, cuda
 
 // ---------------------------------------------------------------- bulk copies
 // Bulk copies (cp.async.bulk) into shared memory with completion counted on
-// an mbarrier.  Every wait on an mbarrier gives up after kSpinLimit tries and
-// the kernel then sets GDEM_EW_TIMEOUT.
-constexpr unsigned kSpinLimit = 1u << 22;
+// an mbarrier.  Every wait on an mbarrier gives up after kSpinLimit tries
+// (View::wait_tries for the pipeline waits) and the kernel then sets
+// GDEM_EW_TIMEOUT.  After a pipeline wait gave up, the waits for the copies
+// still in flight keep the full kSpinLimit, so no CTA leaves a copy
+// outstanding when its shared memory goes away.
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
     return (unsigned)__cvta_generic_to_shared(p);
@@ -762,8 +764,9 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned 
         : "memory");
     return ok != 0u;
 }
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity) {
-    for (unsigned k = 0; k < kSpinLimit; k++)
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity,
+                                                  unsigned tries = kSpinLimit) {
+    for (unsigned k = 0; k < tries; k++)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
@@ -855,7 +858,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_step_mixed_wtma(View<Mixed> v, cu
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             issue_sub(v, A, P, tn, &stage[b ^ 1], &full[warp][b ^ 1], nei_rows);
         }
-        const bool ok = mbar_wait_bounded(&full[warp][b], (unsigned)(it >> 1) & 1u);
+        const bool ok = mbar_wait_bounded(&full[warp][b], (unsigned)(it >> 1) & 1u, v.wait_tries);
         if (__any_sync(0xffffffffu, !ok)) {
             timed_out = true;
             break;
@@ -1033,7 +1036,7 @@ __global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             issue_csub(v, A, P, tn, &stage[b ^ 1], &full[warp][b ^ 1], nei_rows, hid_rows);
         }
-        const bool ok = mbar_wait_bounded(&full[warp][b], (unsigned)(it >> 1) & 1u);
+        const bool ok = mbar_wait_bounded(&full[warp][b], (unsigned)(it >> 1) & 1u, v.wait_tries);
         if (__any_sync(0xffffffffu, !ok)) {
             timed_out = true;
             break;

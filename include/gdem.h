@@ -263,6 +263,12 @@ int gdem_save_snapshot(gdem_handle* h, const char* path);
  * count, precision and model, with its mesh set; the run continues bit for
  * bit as if it had not stopped. */
 int gdem_load_snapshot(gdem_handle* h, const char* path);
+/* Check a snapshot file without a device: its header, its exact length,
+ * history counts within the stored capacities, and every history key an index
+ * of the stored state (partner particles in [0, n)) or of a mesh of n_tri
+ * triangles.  GDEM_OK or GDEM_ERR_ARG.  gdem_load_snapshot runs the same check
+ * before it uploads anything. */
+int gdem_check_snapshot(const char* path, int n_tri);
 int gdem_stats_get(gdem_handle* h, gdem_stats* s);
 
 /* ---- the hot-path stages, callable one at a time ---- */
@@ -302,7 +308,9 @@ int gdem_sort_keys(const uint32_t* keys, int n, uint32_t* keys_sorted, int* perm
  * work is enqueued on `stream` (a cudaStream_t; NULL = legacy default stream)
  * without waiting for it.  The scratch is one fixed array per device, looked
  * up on the first call on that device: make that first call before any stream
- * capture begins.  Calls on one device must not overlap on the GPU (they share
+ * capture begins.  The address is kept with the id of its context; after the
+ * context is torn down (cudaDeviceReset) the next call looks it up again, so
+ * make that call before any capture too.  Calls on one device must not overlap on the GPU (they share
  * the scratch).  d_keys may equal d_keys_sorted; d_perm must not overlap
  * either.  GDEM_ERR_CAPACITY when n > GDEM_SORT_NOALLOC_MAX_KEYS.
  * No counterpart in the reference: it is for callers that must not allocate

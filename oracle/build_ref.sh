@@ -8,10 +8,18 @@
 # Flags follow the reference makefile (makefile:3-5) with the two changes the
 # oracle needs: host code without FMA contraction (-ffp-contract=off) and a
 # CUDA-13-accepted virtual arch for the device code it carries but never runs.
+#
+# `build_ref.sh --where` prints the reference checkout this recipe uses
+# (GDEM_REFERENCE_DIR, else the default below) and nothing when it is absent;
+# the scripts and tests that read reference files ask it.
 set -euo pipefail
 REF="${GDEM_REFERENCE_DIR:-/root/reference}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
+if [ "${1:-}" = "--where" ]; then
+  if [ -f "$REF/cpu_dem.cu" ]; then echo "$REF"; fi
+  exit 0
+fi
 if [ ! -f "$REF/cpu_dem.cu" ]; then
   echo "build_ref: no reference sources at $REF; skipping"
   exit 0

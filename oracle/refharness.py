@@ -17,6 +17,14 @@ MAX_NEI = 100
 _lib = None
 
 
+def reference_dir():
+    """The reference checkout oracle/build_ref.sh builds from (its
+    GDEM_REFERENCE_DIR or default), or None where it is absent."""
+    r = subprocess.run(["bash", os.path.join(HERE, "build_ref.sh"), "--where"], capture_output=True, text=True)
+    where = r.stdout.strip()
+    return where or None
+
+
 def available() -> bool:
     return os.path.exists(LIB_PATH)
 

@@ -74,4 +74,12 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) > 1:
+        root = sys.argv[1]
+    else:
+        sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))))
+        from oracle.refharness import reference_dir
+        root = reference_dir()
+        if root is None:
+            sys.exit("no reference checkout (set GDEM_REFERENCE_DIR or pass its root)")
+    main(root)

@@ -123,6 +123,39 @@ def test_snapshot_refuses_another_engine(tmp_path):
         E.load_snapshot(path)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_snapshot_with_a_corrupt_history_key_is_refused(tmp_path, precision):
+    """A partner id outside [0, n) in a saved snapshot is refused on the host
+    before anything is uploaded: the engine that tried to load it goes on
+    exactly as an engine that never saw the file."""
+    import struct
+    from gpudem_gb300 import _lib, engine, scenes
+    sc = scenes.config3_helical_chute(n=5_000, n_tri=2_000, v_sigma=0.5)
+    path = str(tmp_path / "snap.bin")
+    A = engine.Engine(sc, precision=precision, model="hertz_mindlin")
+    A.step(200)
+    A.save_snapshot(path)
+    assert _lib.load().gdem_check_snapshot(path.encode(), A.ntri) == 0
+    raw = bytearray(open(path, "rb").read())
+    n = sc.n
+    state = n * (7 * 16 if precision == "mixed" else 4 * 32)
+    counts = np.frombuffer(bytes(raw[56 + state:56 + state + 4 * n]), np.int32)
+    assert counts.sum() > 0
+    first_key = 56 + state + 4 * n
+    raw[first_key:first_key + 4] = struct.pack("<i", n + 7)
+    bad = str(tmp_path / "bad.bin")
+    open(bad, "wb").write(bytes(raw))
+    B = engine.Engine(sc, precision=precision, model="hertz_mindlin")
+    C = engine.Engine(sc, precision=precision, model="hertz_mindlin")
+    with pytest.raises(_lib.GdemError, match="history partner"):
+        B.load_snapshot(bad)
+    B.step(50)
+    C.step(50)
+    b, c = B.export(history=True), C.export(history=True)
+    for key in ("x", "v", "angv", "numCont", "indHis", "deltHisx"):
+        assert np.array_equal(b[key], c[key]), key
+
+
 def test_async_position_exports_hold_their_steps():
     """gdem_export_positions_async: each copy holds the positions of the step
     it was queued after, though later steps ran meanwhile."""
