@@ -284,6 +284,8 @@ def run_engine(args):
         extra.update({"fp64_value": fval, "fp64_steps": fsteps, "mixed_over_fp64": value / fval})
         if args.error_steps > 0:
             extra.update(position_error(sc, kw, args.error_steps))
+    if args.workload == "poured" and not args.no_extra:
+        extra.update(extra_lines(args, sc, kw, rebuild_ms))
     # end to end through the C ABI with host buffers
     e2e = run_e2e(args, sc, kw) if not args.no_e2e else None
     out = {
@@ -324,6 +326,54 @@ def run_engine(args):
     }
     if rank == 0:
         print(json.dumps(out))
+
+
+def extra_lines(args, sc, kw, rebuild_ms):
+    """Context lines beside the settled-bed value, each on the same engine
+    and GPU:
+    * the pour itself, with list rebuilds in the timed steps: the chute's
+      inlet state poured for `pour_pre_steps` steps at dt = 2e-5 s (e = 0.1),
+      then timed at the workload's dt = 1e-6 s, and timed at the pour's own
+      dt = 2e-5 s (a list rebuild every few steps);
+    * the linear contact law (the reference's only one) in mixed precision and
+      in FP64 on the settled bed, the like-for-like partner of the reference
+      arm's CPU path;
+    * the mixed step scanning the list rows instead of the inner rows, which
+      splits the mixed/FP64 ratio into precision and algorithm."""
+    import torch
+    from dataclasses import replace
+    from gpudem_gb300 import engine, scenes
+    out = {}
+
+    def timed(scene, precision, steps, tag, **over):
+        E = engine.Engine(scene, precision=precision, **dict(kw, **over))
+        ms, a0, a1 = _time_steps(E, steps, args.warmup, torch.cuda.ExternalStream(E.stream()), tag=tag)
+        E.close()
+        n_act = 0.5 * (a0["n_active"] + a1["n_active"])
+        return {"value": n_act * steps / (ms / 1e3), "ms_per_step": ms / steps, "steps": steps,
+                "rebuilds": int(a1["rebuilds"] - a0["rebuilds"]),
+                "inner_builds": int(a1["inner_builds"] - a0["inner_builds"])}
+
+    mid = scenes.settle_scene(scenes.config3_chute_pour(n=args.n, n_tri=args.ntri), steps=args.pour_pre_steps)
+    for tag, scene, steps in (("pour_dt1e-6", mid, args.steps),
+                              ("pour_dt2e-5", replace(mid, dt=2e-5, e=0.1), max(50, args.steps // 4))):
+        r = timed(scene, args.precision, steps, "timed_" + tag)
+        # share of the timed region spent in list rebuilds (each as long as
+        # the forced rebuild timed on the settled bed)
+        r["rebuild_share"] = round(min(1.0, r["rebuilds"] * rebuild_ms / (r["ms_per_step"] * steps)), 4)
+        r["state"] = f"chute inlet poured {args.pour_pre_steps} steps at dt=2e-5 s, e=0.1"
+        out[tag] = r
+    fsteps = max(10, args.steps // 4)
+    lin_mixed = timed(sc, "mixed", args.steps, "timed_linear_mixed", model="linear")
+    lin_fp64 = timed(sc, "fp64", fsteps, "timed_linear_fp64", model="linear")
+    out["linear_model"] = {"mixed_value": lin_mixed["value"], "fp64_value": lin_fp64["value"],
+                           "mixed_over_fp64": lin_mixed["value"] / lin_fp64["value"],
+                           "note": "the reference's contact law, same bed; the reference arm times it in FP64 on "
+                                   "the host cores"}
+    if args.precision == "mixed":
+        out["mixed_no_inner_value"] = timed(sc, "mixed", max(10, args.steps // 2), "timed_no_inner",
+                                            inner_skin=-1.0)["value"]
+    return out
 
 
 def position_error(sc, kw, steps):
@@ -417,13 +467,44 @@ def cpu_baseline(args, sc):
     return out
 
 
+_BED_FIELDS = ("x", "r", "m", "k", "eta", "mu", "dt", "tris", "inlet_lo", "inlet_hi", "g", "v", "w", "skin",
+               "refresh", "E", "nu", "e", "mu_roll", "active")
+
+
+def save_bed(args):
+    """Write the workload's scene (the bed the engine arm steps) to
+    args.save_bed; run in a process of its own by the reference arm."""
+    sc, _ = workload(args)
+    np.savez(args.save_bed, **{f: np.asarray(getattr(sc, f)) for f in _BED_FIELDS if getattr(sc, f) is not None})
+
+
+def load_bed(args):
+    """The engine arm's bed, prepared by a separate process (the GPU pour), so
+    that the reference arm's own process maps no part of the engine."""
+    from gpudem_gb300.scenes import Scene
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "bed.npz")
+        cmd = [sys.executable, os.path.abspath(__file__), "--save-bed", path, "--workload", args.workload,
+               "--n", str(args.n), "--ntri", str(args.ntri), "--settle-steps", str(args.settle_steps),
+               "--v-sigma", str(args.v_sigma)]
+        subprocess.run(cmd, check=True)
+        z = dict(np.load(path))
+    scal = {f: float(z[f]) for f in ("mu", "dt", "skin", "refresh", "E", "nu", "e", "mu_roll")}
+    return Scene(x=z["x"], r=z["r"], m=z["m"], k=z["k"], eta=z["eta"], tris=z["tris"], inlet_lo=z["inlet_lo"],
+                 inlet_hi=z["inlet_hi"], g=z["g"], v=z.get("v"), w=z.get("w"), active=z.get("active"), **scal)
+
+
 def run_reference(args):
     dist, rank, ws = dist_init()
     if rank != 0:
         return
-    # the same bed as the engine arm: poured (settled) by the engine on the GPU
-    # as input preparation; the timed steps run the CPU path only
-    sc, _ = workload(args)
+    # the same bed as the engine arm, poured by the engine on the GPU in a
+    # separate process as input preparation; this process runs the CPU path only
+    try:
+        sc = load_bed(args)
+    except Exception as e:  # noqa: BLE001
+        print(json.dumps({"impl": "reference", "unavailable": f"bed preparation failed: {e}"}))
+        return
     try:
         from oracle import port
         res = port.time_steps(active_only(sc), steps=args.steps, warmup=args.warmup, budget_s=args.cpu_budget)
@@ -538,6 +619,11 @@ def parse_args(argv=None):
     ap.add_argument("--settle-steps", type=int, default=12000)
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the pour, linear-model and list-row context lines")
+    ap.add_argument("--pour-pre-steps", type=int, default=3000,
+                    help="steps at dt=2e-5 s from the chute inlet to the pouring state of the pour lines")
+    ap.add_argument("--save-bed", default=None, help=argparse.SUPPRESS)
     ap.add_argument("--clocks-dir", default=None,
                     help="where the nvidia-smi clock samples of the timed region go (default: the temp dir)")
     args = ap.parse_args(argv)
@@ -560,7 +646,9 @@ def parse_args(argv=None):
 
 def main():
     args = parse_args()
-    if args.impl == "reference":
+    if args.save_bed:
+        save_bed(args)
+    elif args.impl == "reference":
         run_reference(args)
     elif args.workload == "batched":
         run_batched(args)

@@ -35,6 +35,7 @@ UNITS = {
     "gdem_noalloc.cu": True,
     "gdem_output.cu": True,
     "gdem_init.cu": True,
+    "gdem_settings.cpp": True,
 }
 # the mixed-precision step: FP32 contact law with the hardware's approximate
 # reciprocal and square root (its error is measured against the FP64 mode)
@@ -69,7 +70,7 @@ def build_engine(verbose=False, ptxas_info=False) -> str:
     jobs = []
     for unit, nofma in UNITS.items():
         src = os.path.join(CSRC, unit)
-        obj = os.path.join(OUT, unit.replace(".cu", ".o"))
+        obj = os.path.join(OUT, os.path.splitext(unit)[0] + ".o")
         objs.append(obj)
         if _stale(obj, [src, *headers, __file__]):
             cmd = [nvcc, *ARCH, *COMMON, "-fmad=false" if nofma else "-fmad=true", *EXTRA.get(unit, []), "-c", src,

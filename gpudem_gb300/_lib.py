@@ -24,6 +24,7 @@ EXPORTED = [
     "gdem_dist_triangle", "gdem_export_mesh", "gdem_get_stream", "gdem_profile_step",
     "gdem_export_positions", "gdem_frame_write_async", "gdem_frames_flush", "gdem_save_snapshot",
     "gdem_load_snapshot", "gdem_init_particles", "gdem_export_positions_async", "gdem_check_snapshot",
+    "gdem_settings_load", "gdem_settings_parse", "gdem_read_particle_file", "gdem_read_stl",
 ]
 PLACE = {"random": 0, "lattice": 1}
 RADIUS = {"mono": 0, "uniform": 1, "lognormal": 2, "bidisperse": 3}
@@ -36,6 +37,22 @@ class Inlet(C.Structure):
                 ("r_d", C.c_double), ("density", C.c_double), ("youngs_modulus", C.c_double),
                 ("restitution", C.c_double), ("velocity", C.c_double * 3), ("velocity_sigma", C.c_double),
                 ("gap", C.c_double), ("seed", C.c_ulonglong)]
+
+
+SETTINGS_MAX_WALLS, SETTINGS_PATH = 16, 1024
+INLET_SHUFFLE, INLET_FILE = 0, 1
+
+
+class Settings(C.Structure):
+    """gdem_settings: demSettings.json as main.cu reads it."""
+    _fields_ = [("radius", C.c_double), ("restitution", C.c_double), ("density", C.c_double), ("mu", C.c_double),
+                ("youngs_modulus", C.c_double), ("k_given", C.c_double), ("mass", C.c_double),
+                ("stiffness", C.c_double), ("etaconst", C.c_double), ("dt", C.c_double), ("out_step", C.c_int),
+                ("n_particles", C.c_int), ("input_mode", C.c_int), ("inlet_min", C.c_double * 3),
+                ("inlet_max", C.c_double * 3), ("particle_file", C.c_char * SETTINGS_PATH), ("n_walls", C.c_int),
+                ("walls", (C.c_char * SETTINGS_PATH) * SETTINGS_MAX_WALLS), ("g", C.c_double * 3),
+                ("gpu_on", C.c_int), ("brute_on", C.c_int), ("seed", C.c_int), ("dt_factor", C.c_double),
+                ("start_time", C.c_double), ("end_time", C.c_double), ("output_timing", C.c_double)]
 
 
 class MeshArrays(C.Structure):
@@ -139,6 +156,10 @@ def load(build_if_missing: bool = False):
     L.gdem_save_snapshot.argtypes = [vp, C.c_char_p]
     L.gdem_load_snapshot.argtypes = [vp, C.c_char_p]
     L.gdem_check_snapshot.argtypes = [C.c_char_p, C.c_int]
+    L.gdem_settings_load.argtypes = [C.c_char_p, C.POINTER(Settings), C.c_char_p, C.c_int]
+    L.gdem_settings_parse.argtypes = [C.c_char_p, C.POINTER(Settings), C.c_char_p, C.c_int]
+    L.gdem_read_particle_file.argtypes = [C.c_char_p, C.c_int, vp, vp, vp, vp]
+    L.gdem_read_stl.argtypes = [C.c_char_p, vp, C.c_int]
     L.gdem_init_particles.argtypes = [vp, C.POINTER(Inlet)]
     L.gdem_export_positions_async.argtypes = [vp, vp]
     for nm in EXPORTED:

@@ -314,6 +314,7 @@ struct Impl : EngineBase {
             A.add(&v.ftmp, (size_t)6 * n);
         }
         if (T::mixed) A.add(&v.inv, n);
+        A.add(&v.where, n);
         A.add(&v.rs_hist, (size_t)256 * v.rs_blocks);
         A.add(&v.rs_tot, 256);
         A.add(&v.ctl, 1);

@@ -145,9 +145,12 @@ __device__ double sample_radius(const gdem_inlet& in, uint64_t seed, int i) {
 // vals[i], its radius, mass (rho * 3.14 * r^3 * 4/3 in main.cu:67's order),
 // linear stiffness and damping constant (ParticleSystem.cu:202, :301) and
 // velocity.
+// log_res is ln(restitution) from the host's C library, the log the
+// reference's initializeParticles calls, so that the damping constant matches
+// it bit for bit (the device log may round differently).
 __global__ void k_make_particles(gdem_inlet in, int n, double rmax, const int* vals, const double4* cells,
                                  long long sx, long long sy, double* x, double* v, double* r, double* m, double* k,
-                                 double* eta) {
+                                 double* eta, double log_res) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint64_t seed = in.seed;
@@ -176,7 +179,7 @@ __global__ void k_make_particles(gdem_inlet in, int n, double rmax, const int* v
     const double E = in.youngs_modulus;
     const double ki = 4. / 3. * (E * 0.5) * sqrt(ri * 0.5) * sqrt(0.05 * ri);
     k[i] = ki;
-    const double le = log(in.restitution);
+    const double le = log_res;
     eta[i] = -2. * le * sqrt(ki / (3.1415 * 3.1415 + le * le));
     for (int a = 0; a < 3; a++)
         v[3 * i + a] = in.velocity[a] + (in.velocity_sigma > 0. ? in.velocity_sigma * gauss(seed, kVel, 3 * (uint64_t)i + a) : 0.);
@@ -290,7 +293,8 @@ int init_particles_device(const gdem_inlet& in, int n, double* x, double* v, dou
         else
             k_cell_keys<<<(unsigned)((nitems + B - 1) / B), B, 0, st>>>(cells, nitems, keys0, vals0, in.seed);
         radix_sort_pairs(keys0, vals0, keys1, vals1, hist, tot, (int)nitems, nb, 0, 4, st);
-        k_make_particles<<<(n + B - 1) / B, B, 0, st>>>(in, n, rmax, vals0, cells, sx, sy, x, v, r, m, k, eta);
+        k_make_particles<<<(n + B - 1) / B, B, 0, st>>>(in, n, rmax, vals0, cells, sx, sy, x, v, r, m, k, eta,
+                                                         std::log(in.restitution));
         CKI(cudaGetLastError());
         CKI(cudaStreamSynchronize(st));
     }

@@ -198,6 +198,7 @@ struct View {
     uint32_t* keys[2];
     int* vals[2];
     int* inv;                        // mixed mode: old storage index -> new, at a reorder
+    int* where;                      // storage index of each pId (set with the cell ranges)
     uint32_t* rs_hist;               // [256 * rs_blocks]
     uint32_t* rs_tot;                // [256]
     int rs_blocks;

@@ -251,7 +251,7 @@ __global__ void k_inverse_order(View<T> v, int gated) {
 // Gather every per-particle array into sorted order (d_swap_ps,
 // BoundingBox.cu:928-1005, but with compact histories: only live slots move).
 template <class T>
-__global__ void k_reorder(View<T> v, int gated) {
+__global__ void __launch_bounds__(kBlock, 4) k_reorder(View<T> v, int gated) {
     Ctl* ctl = v.ctl;
     if (gated && ctl->refresh == 0u) return;
     const int s = ctl->s, p = ctl->p;
@@ -272,20 +272,53 @@ __global__ void k_reorder(View<T> v, int gated) {
         const PBank<T> P = v.P[p], Q = v.P[p ^ 1];
         Q.mat[i] = P.mat[src];
         Q.pid[i] = P.pid[src];
+        // live history slots, four at a time with their loads in flight
+        // together (the slot rows are slot-major: slot k of particle i at
+        // k * n + i, so a warp's loads of one slot are contiguous)
+        using R = typename T::real;
         const int nc = P.nc[src];
         Q.nc[i] = nc;
-        for (int k = 0; k < nc; k++) {
-            const size_t a = (size_t)k * n + src, b = (size_t)k * n + i;
-            Q.hid[b] = T::mixed ? v.inv[P.hid[a]] : P.hid[a];
-            Q.hx[b] = P.hx[a]; Q.hy[b] = P.hy[a]; Q.hz[b] = P.hz[a];
-            if (T::mixed) { Q.cx[b] = P.cx[a]; Q.cy[b] = P.cy[a]; Q.cz[b] = P.cz[a]; }
+        for (int k0 = 0; k0 < nc; k0 += 4) {
+            int id[4];
+            R t[6][4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                if (k0 + q >= nc) continue;
+                const size_t a = (size_t)(k0 + q) * n + src;
+                id[q] = P.hid[a];
+                t[0][q] = P.hx[a]; t[1][q] = P.hy[a]; t[2][q] = P.hz[a];
+                if (T::mixed) { t[3][q] = P.cx[a]; t[4][q] = P.cy[a]; t[5][q] = P.cz[a]; }
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                if (k0 + q >= nc) continue;
+                const size_t b = (size_t)(k0 + q) * n + i;
+                Q.hid[b] = T::mixed ? v.inv[id[q]] : id[q];
+                Q.hx[b] = t[0][q]; Q.hy[b] = t[1][q]; Q.hz[b] = t[2][q];
+                if (T::mixed) { Q.cx[b] = t[3][q]; Q.cy[b] = t[4][q]; Q.cz[b] = t[5][q]; }
+            }
         }
         const int ncw = P.ncw[src];
         Q.ncw[i] = ncw;
-        for (int k = 0; k < ncw; k++) {
-            const size_t a = (size_t)k * n + src, b = (size_t)k * n + i;
-            Q.hwid[b] = P.hwid[a]; Q.hwx[b] = P.hwx[a]; Q.hwy[b] = P.hwy[a]; Q.hwz[b] = P.hwz[a];
-            if (T::mixed) { Q.cwx[b] = P.cwx[a]; Q.cwy[b] = P.cwy[a]; Q.cwz[b] = P.cwz[a]; }
+        for (int k0 = 0; k0 < ncw; k0 += 2) {
+            int id[2];
+            R t[6][2];
+#pragma unroll
+            for (int q = 0; q < 2; q++) {
+                if (k0 + q >= ncw) continue;
+                const size_t a = (size_t)(k0 + q) * n + src;
+                id[q] = P.hwid[a];
+                t[0][q] = P.hwx[a]; t[1][q] = P.hwy[a]; t[2][q] = P.hwz[a];
+                if (T::mixed) { t[3][q] = P.cwx[a]; t[4][q] = P.cwy[a]; t[5][q] = P.cwz[a]; }
+            }
+#pragma unroll
+            for (int q = 0; q < 2; q++) {
+                if (k0 + q >= ncw) continue;
+                const size_t b = (size_t)(k0 + q) * n + i;
+                Q.hwid[b] = id[q];
+                Q.hwx[b] = t[0][q]; Q.hwy[b] = t[1][q]; Q.hwz[b] = t[2][q];
+                if (T::mixed) { Q.cwx[b] = t[3][q]; Q.cwy[b] = t[4][q]; Q.cwz[b] = t[5][q]; }
+            }
         }
     }
     if (last_block(&ctl->done[1])) {
@@ -341,6 +374,9 @@ __global__ void k_cell_ranges(View<T> v, int gated) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = v.n;
     if (q >= n) return;
+    // storage index of every pId (the Verlet rows are built as pIds)
+    const int jq = v.reorder ? q : v.vals[0][q];
+    v.where[v.P[ctl->p].pid[jq]] = jq;
     const uint32_t* key = v.keys[0];
     const uint32_t kq = key[q];
     if (kq == kNoKey) return;
@@ -378,8 +414,21 @@ __global__ void k_posf(View<T> v, int gated) {
 // roundings of the coordinates), and only a candidate whose FP32 distance is
 // within that band of the cutoff takes the FP64 test.  The decision is the
 // FP64 test's in every case.
+//
+// The row grows in shared memory as partner pIds kept sorted by insertion
+// (slot k of thread t at k * kNbBlock + t: the threads of a warp touch 32
+// banks), and is written out once, mapped back to storage indices through
+// v.where, slot by slot (a warp writes 32 consecutive ints per slot).
+constexpr int kNbBlock = 128;
+
+template <int CAP>
+constexpr size_t nb_smem_bytes() {
+    return sizeof(int) * (size_t)CAP * kNbBlock;
+}
+
 template <class T, int CAP>
-__global__ void __launch_bounds__(kBlock) k_neighbors(View<T> v, int gated) {
+__global__ void __launch_bounds__(kNbBlock) k_neighbors(View<T> v, int gated) {
+    extern __shared__ int nb_rows[];
     Ctl* ctl = v.ctl;
     if (gated && ctl->refresh == 0u) return;
     const int n = v.n;
@@ -388,6 +437,8 @@ __global__ void __launch_bounds__(kBlock) k_neighbors(View<T> v, int gated) {
     const SBank<T> S = v.S[s];
     const PBank<T> P = v.P[p];
     const float4* __restrict__ PF = T::mixed ? S.posh : v.posf;
+    const int* __restrict__ pidv = P.pid;
+    int* row = nb_rows + threadIdx.x;
     int count = 0;
     if (i < n) {
         if (S.rot[i].w == 0) {
@@ -398,11 +449,10 @@ __global__ void __launch_bounds__(kBlock) k_neighbors(View<T> v, int gated) {
             const double xi = pi.x, yi = pi.y, zi = pi.z, ri = pi.w;
             const double skin = v.skin;
             const float skinf = (float)v.skin, delta = v.nb_delta;
+            const float rfi = fabsf(fi.w) + skinf;
             const int cx = cell_x(v, xi);
             const int cy = cell_coord(yi, v.miny, v.invdy);
             const int cz = cell_coord(zi, v.minz, v.invdz);
-            int cand_pid[CAP];
-            int cand_j[CAP];
             bool overflow = false;
             for (int sz = -1; sz <= 1; sz++) {
                 const int zz = cz + sz;
@@ -427,9 +477,10 @@ __global__ void __launch_bounds__(kBlock) k_neighbors(View<T> v, int gated) {
                             const float4 fj = PF[j];
                             const float ex = image_dxf(v, fi.x - fj.x), ey = fi.y - fj.y, ez = fi.z - fj.z;
                             const float dsqf = ex * ex + ey * ey + ez * ez;
-                            const float Rf = fabsf(fi.w) + fabsf(fj.w) + skinf;
-                            const float Rhi = Rf + delta, Rlo = Rf - delta;
+                            const float Rf = rfi + fabsf(fj.w);
+                            const float Rhi = Rf + delta;
                             if (dsqf > Rhi * Rhi * 1.0000039f) continue;  // (1 + 2^-18): surely outside
+                            const float Rlo = Rf - delta;
                             bool inside = Rlo > 0.f && dsqf < Rlo * Rlo * 0.9999962f;  // surely inside
                             if (!inside) {
                                 const double4_32a pj = load_pos(S, j);
@@ -441,20 +492,20 @@ __global__ void __launch_bounds__(kBlock) k_neighbors(View<T> v, int gated) {
                                 inside = distsq < R * R;
                             }
                             if (inside) {
-                                const int pid_j = P.pid[j];
                                 if (count >= CAP) {
                                     overflow = true;
                                     continue;
                                 }
                                 // insertion by pId keeps the row sorted as it grows
+                                const int pid_j = pidv[j];
                                 int k = count;
-                                while (k > 0 && cand_pid[k - 1] > pid_j) {
-                                    cand_pid[k] = cand_pid[k - 1];
-                                    cand_j[k] = cand_j[k - 1];
+                                while (k > 0) {
+                                    const int prev = row[(k - 1) * kNbBlock];
+                                    if (prev < pid_j) break;
+                                    row[k * kNbBlock] = prev;
                                     k--;
                                 }
-                                cand_pid[k] = pid_j;
-                                cand_j[k] = j;
+                                row[k * kNbBlock] = pid_j;
                                 count++;
                             }
                         }
@@ -463,7 +514,7 @@ __global__ void __launch_bounds__(kBlock) k_neighbors(View<T> v, int gated) {
             }
             if (overflow || count > v.nei_cap) atomicOr(&ctl->error, 0x1u);
             const int m = count < v.nei_cap ? count : v.nei_cap;
-            for (int k = 0; k < m; k++) v.nei[(size_t)k * n + i] = cand_j[k];
+            for (int k = 0; k < m; k++) v.nei[(size_t)k * n + i] = v.where[row[k * kNbBlock]];
             v.nnei[i] = m;
             if (T::mixed)
                 v.refh[i] = make_float4(fi.x, fi.y, fi.z, 0.f);
@@ -475,6 +526,17 @@ __global__ void __launch_bounds__(kBlock) k_neighbors(View<T> v, int gated) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) wmax = max(wmax, __shfl_xor_sync(0xffffffffu, wmax, o));
     if ((threadIdx.x & 31) == 0 && wmax > 0) atomicMax(&ctl->max_nei, wmax);
+}
+
+template <class T, int CAP>
+static void launch_neighbors(const View<T>& v, int gated, cudaStream_t st) {
+    static bool configured = false;
+    if (!configured) {
+        cudaFuncSetAttribute(k_neighbors<T, CAP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)nb_smem_bytes<CAP>());
+        configured = true;
+    }
+    k_neighbors<T, CAP><<<(v.n + kNbBlock - 1) / kNbBlock, kNbBlock, nb_smem_bytes<CAP>(), st>>>(v, gated);
 }
 
 // ===================================================================== wall lists
@@ -739,11 +801,11 @@ void launch_rebuild(const View<T>& v, cudaStream_t st, int force) {
     k_cell_ranges<T><<<g, kBlock, 0, st>>>(v, gated);
     if constexpr (!T::mixed) k_posf<T><<<g, kBlock, 0, st>>>(v, gated);
     if (v.nei_cap <= 32)
-        k_neighbors<T, 32><<<g, kBlock, 0, st>>>(v, gated);
+        launch_neighbors<T, 32>(v, gated, st);
     else if (v.nei_cap <= 64)
-        k_neighbors<T, 64><<<g, kBlock, 0, st>>>(v, gated);
+        launch_neighbors<T, 64>(v, gated, st);
     else
-        k_neighbors<T, 128><<<g, kBlock, 0, st>>>(v, gated);
+        launch_neighbors<T, 128>(v, gated, st);
     if (v.wall_cap <= 16)
         k_wall_lists<T, 16><<<g, kBlock, 0, st>>>(v, gated);
     else if (v.wall_cap <= 32)

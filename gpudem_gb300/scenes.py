@@ -311,18 +311,29 @@ def config1_box_drop(n=100, seed=1) -> Scene:
                  e=0.5, name="box-drop-100")
 
 
-def config2_tilted_box(n=30_000, seed=2, r0=2e-3, half=0.1, levels=0, linear_k=None) -> Scene:
+def config2_tilted_box(n=30_000, seed=2, r0=2e-3, half=None, levels=0, linear_k=None) -> Scene:
     """Spheres with r ~ U[0.8,1.2]*r0 at seeded random packing in the upper part
     of a closed box tilted 30 degrees (12 triangles).  The Hertz-Mindlin
     material is E=5e6 Pa, nu=0.3, e=0.6, mu=0.4, dt=2e-6 s; `linear_k` (or the
-    reference's k(E, r0) law) gives the linear-model twin."""
+    reference's k(E, r0) law) gives the linear-model twin.  `half` (the box's
+    half-width) defaults to 0.1 m, widened in steps of 0.025 m until the
+    upper region holds the spheres (0.15 m for 30,000)."""
     rng = np.random.default_rng(seed)
     radii = r0 * rng.uniform(0.8, 1.2, n)
-    # the tilted cube of half-width `half` contains the axis-aligned cube of
-    # half-width half/(cos30+sin30) around its centre
-    s = half / (math.cos(math.radians(30)) + math.sin(math.radians(30)))
-    lo = np.array([-s, -0.2 * s, -s])
-    hi = np.array([s, s, s])
+    cs = math.cos(math.radians(30)) + math.sin(math.radians(30))
+
+    def region(h):
+        # the tilted cube of half-width h contains the axis-aligned cube of
+        # half-width h/(cos30+sin30) around its centre
+        s = h / cs
+        return np.array([-s, -0.2 * s, -s]), np.array([s, s, s])
+
+    if half is None:
+        half = 0.1
+        a = 2.0 * radii.max() * 1.05
+        while n > 5000 and np.prod(np.floor((region(half)[1] - region(half)[0] - 2 * radii.max()) / a) + 1) < n:
+            half += 0.025
+    lo, hi = region(half)
     x = lattice_packing(n, radii, lo, hi, rng, gap=0.05) if n > 5000 else \
         random_packing(n, radii, lo, hi, rng)
     m = sphere_mass(2500.0, radii)

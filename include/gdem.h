@@ -334,6 +334,61 @@ int gdem_dist_triangle(gdem_handle* h, const double* pos, const double* r, const
 int gdem_export_mesh(gdem_handle* h, double* rec, int* irec, double* aabb, uint32_t* morton,
                      int* sorted_index);
 
+/* ---- settings, particle files and walls (the host side of main.cu) ---- */
+#define GDEM_INLET_SHUFFLE 0
+#define GDEM_INLET_FILE 1
+#define GDEM_SETTINGS_MAX_WALLS 16
+#define GDEM_SETTINGS_PATH 1024
+
+/* demSettings.json as main.cu reads it (main.cu:44-140; keys in the comments).
+ * Numbers the file does not give are NAN where noted. */
+typedef struct gdem_settings {
+    /* particleTypes.particle0 */
+    double radius, restitution, density, mu;  /* radius, CoR, density, mu */
+    double youngs_modulus;                    /* YoungModulus; NAN when absent */
+    double k_given;                           /* k; NAN when absent */
+    /* derived in the reference's operation order */
+    double mass;        /* density * 3.14 * r^3 * 4/3 (main.cu:67) */
+    double stiffness;   /* 4/3 (E/2) sqrt(r/2) sqrt(0.05 r) (ParticleSystem.cu:202), or k when E is absent */
+    double etaconst;    /* -2 ln e sqrt(k / (3.1415^2 + ln^2 e)) (ParticleSystem.cu:301) */
+    double dt;          /* 2 PI sqrt(m/k) / dtFactor, snapped to outputTiming / out_step (main.cu:123-129) */
+    int out_step;       /* steps per output interval */
+    /* inlet */
+    int n_particles;    /* numParticle */
+    int input_mode;     /* inputMode: GDEM_INLET_SHUFFLE or GDEM_INLET_FILE */
+    double inlet_min[3], inlet_max[3];          /* the shuffle box (file mode: NAN; see gdem_read_particle_file) */
+    char particle_file[GDEM_SETTINGS_PATH];     /* file mode: the particle file */
+    /* walls.filepaths */
+    int n_walls;
+    char walls[GDEM_SETTINGS_MAX_WALLS][GDEM_SETTINGS_PATH];
+    double g[3];        /* gravity.x/y/z */
+    /* others */
+    int gpu_on, brute_on, seed;                 /* gpuOn; bruteOn (default 0); seed (default 1) */
+    double dt_factor, start_time, end_time, output_timing;  /* dtFactor, startTime (default 0), endTime,
+                                                               outputTiming */
+} gdem_settings;
+
+/* Read demSettings.json (replaces load_json_file and the reads of main.cu:44-140,
+ * settings_loader.cu).  Unlike the reference: YoungModulus may be absent (the
+ * shipped cases give "k", used as is), bruteOn may be absent (0), and the
+ * "file" inlet takes its file name as a string or as {"name": ...} (the
+ * reference's string getter accepts only objects, cJSON_d.c:3226-3232).
+ * Missing or mistyped keys give GDEM_ERR_ARG and their path in msg (up to
+ * msg_len bytes) instead of abort(). */
+int gdem_settings_load(const char* path, gdem_settings* s, char* msg, int msg_len);
+/* The same from the JSON text itself. */
+int gdem_settings_parse(const char* json_text, gdem_settings* s, char* msg, int msg_len);
+/* The "file" inlet's particles (ParticleSystem.cu:357-440): a CSV whose header
+ * names the columns x, y, z, vx, vy, vz, then exactly n rows.  x[3n] and v[3n]
+ * (may be NULL) in file order; box_min/box_max (may be NULL) receive the
+ * positions' bounding box, the inlet region of calc_BoundingBoxLimits
+ * (BoundingBox.cu:448). */
+int gdem_read_particle_file(const char* path, int n, double* x, double* v, double* box_min, double* box_max);
+/* Triangles of an ASCII STL file in file order, as load_ascii_stl_double
+ * reads them (TriangleMesh.cu:347-386): 9 doubles per triangle into tris (at
+ * most cap).  Returns the file's triangle count, -1 if unreadable. */
+int gdem_read_stl(const char* path, double* tris, int cap);
+
 /* ---- measurement ---- */
 
 /* The CUDA stream (cudaStream_t) every call of this handle enqueues on, for

@@ -346,6 +346,46 @@ void rh_dist_triangle(void* hv, int i, int j, double* out4, int* hitAt) {
     *hitAt = (tc.dist < 1e9) ? tc.hitAt : -2;
 }
 
+/* The reference's own initializeParticles (ParticleSystem.cu:189-340) on a
+ * "shuffle" inlet of N particles of radius r in [lo, hi], with the mass
+ * main.cu:67 computes from the density (its expression, restated here since
+ * main.cu is not part of the harness) and the Young's modulus and
+ * restitution it passes.  Out: x[3N] and per particle m, k, etaconst, moi,
+ * invmoi, sqrtm, invm. */
+int rh_init_particles(int N, double r, double density, double E, double res, const double* lo, const double* hi,
+                      double* x, double* m, double* k, double* eta, double* moi, double* invmoi, double* sqrtm,
+                      double* invm) {
+    ParticleSys<HostMemory> ps;
+    memset(&ps, 0, sizeof(ps));
+    ps.N = N;
+    allocate(&ps);
+    const double mass = density * 3.14 * r * r * r * 4. / 3.;
+    cJSON* inlet = cJSON_CreateObject();
+    cJSON_AddStringToObject(inlet, "inputMode", "shuffle");
+    cJSON* sh = cJSON_CreateObject();
+    cJSON_AddNumberToObject(sh, "minx", lo[0]);
+    cJSON_AddNumberToObject(sh, "miny", lo[1]);
+    cJSON_AddNumberToObject(sh, "minz", lo[2]);
+    cJSON_AddNumberToObject(sh, "maxx", hi[0]);
+    cJSON_AddNumberToObject(sh, "maxy", hi[1]);
+    cJSON_AddNumberToObject(sh, "maxz", hi[2]);
+    cJSON_AddItemToObject(inlet, "shuffle", sh);
+    initializeParticles(&ps, inlet, r, mass, E, res);
+    cJSON_Delete(inlet);
+    for (int i = 0; i < N; i++) {
+        for (int d = 0; d < 3; d++) x[3 * i + d] = ps.x[3 * i + d];
+        m[i] = ps.m[i];
+        k[i] = ps.k[i];
+        eta[i] = ps.etaconst[i];
+        moi[i] = ps.moi[i];
+        invmoi[i] = ps.invmoi[i];
+        sqrtm[i] = ps.sqrtm[i];
+        invm[i] = ps.invm[i];
+    }
+    deallocate(&ps);
+    return 0;
+}
+
 int rh_step_count(void* hv) { return ((RefHandle*)hv)->step; }
 int rh_num_tri(void* hv) { return ((RefHandle*)hv)->mesh.nTri; }
 int rh_node_count(void* hv) { return ((RefHandle*)hv)->bvh.nodeCount; }

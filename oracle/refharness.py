@@ -68,6 +68,8 @@ def lib():
         L.rh_node_count.restype = C.c_int
         L.rh_node_count.argtypes = [C.c_void_p]
         L.rh_destroy.argtypes = [C.c_void_p]
+        L.rh_init_particles.restype = C.c_int
+        L.rh_init_particles.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, dp, dp] + [dp] * 8
         _lib = L
     return _lib
 
@@ -215,3 +217,13 @@ def radix_sort(keys):
 
 def morton3d(x, y, z):
     return lib().rh_morton3d(int(x), int(y), int(z))
+
+
+def init_particles(n, r, density, E, res, lo, hi):
+    """initializeParticles (ParticleSystem.cu:189-340) of the reference on a
+    shuffle inlet: positions and the per-particle constants it sets."""
+    out = {k: np.zeros(3 * n if k == "x" else n) for k in ("x", "m", "k", "etaconst", "moi", "invmoi", "sqrtm", "invm")}
+    lib().rh_init_particles(int(n), float(r), float(density), float(E), float(res),
+                            np.ascontiguousarray(lo, np.float64), np.ascontiguousarray(hi, np.float64),
+                            *[out[k] for k in ("x", "m", "k", "etaconst", "moi", "invmoi", "sqrtm", "invm")])
+    return out

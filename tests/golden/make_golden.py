@@ -2,7 +2,8 @@
 reference CPU path (oracle/_ref/librefharness.so, built by oracle/build_ref.sh
 from the reference sources).  Run from the repository root:
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py          # every fixture
+    python tests/golden/make_golden.py init     # init_particles.npz only
 
 Every fixture records the exact inputs next to the outputs, so the tests can
 rebuild the same scene for the oracle port and the CUDA engine without the
@@ -208,9 +209,34 @@ def meshes():
     print("meshes.npz", os.path.getsize(os.path.join(OUT, "meshes.npz")) // 1024, "KiB")
 
 
+# (radius, density, Young's modulus, restitution) of the particle-constant
+# fixture: the three workloads' materials (linear twins) and two of the
+# shipped cases' particles with a Young's modulus given
+INIT_CASES = [(0.01, 2500.0, 9.487e7, 0.5), (2e-3, 2500.0, 5e6, 0.6), (1e-3, 2500.0, 5e6, 0.5),
+              (0.01, 1000.0, 1e7, 0.3), (0.1, 1000.0, 1e9, 0.3)]
+
+
+def init_particles():
+    """The reference's initializeParticles (ParticleSystem.cu:189-340) on a
+    40-particle shuffle inlet per material: mass, stiffness, damping constant,
+    moment of inertia and the derived inverses it stores."""
+    out = {"cases": np.array(INIT_CASES)}
+    for c, (r, rho, E, e) in enumerate(INIT_CASES):
+        o = rh.init_particles(40, r, rho, E, e, [-20 * r, 0.0, -20 * r], [20 * r, 20 * r, 20 * r])
+        for k in ("m", "k", "etaconst", "moi", "invmoi", "sqrtm", "invm"):
+            assert np.all(o[k] == o[k][0]), k
+            out[f"c{c}_{k}"] = np.float64(o[k][0])
+    np.savez_compressed(os.path.join(OUT, "init_particles.npz"), **out)
+    print("init_particles.npz", os.path.getsize(os.path.join(OUT, "init_particles.npz")), "B")
+
+
 def main():
     if not rh.available():
         rh.build()
+    if sys.argv[1:] == ["init"]:
+        init_particles()
+        return
+    init_particles()
     components()
     meshes()
     run_case("box_drop_100", scenes.config1_box_drop(), [1, 2, 10, 100, 1000, 5000, 10000, 20000])

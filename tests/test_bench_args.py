@@ -35,3 +35,24 @@ def test_sort_launch_count():
     assert bench.sort_launches(32 * 2048) == 8
     assert bench.sort_launches(32 * 2048 + 1) == 12
     assert bench.sort_launches(1_000_000) == 12
+
+
+def test_reference_arm_loads_the_bed_from_another_process(monkeypatch):
+    """The reference arm takes the engine arm's bed from a file that a
+    separate process writes, and maps no part of the engine itself."""
+    import numpy as np
+    from gpudem_gb300 import _lib, scenes
+    want = scenes.config1_box_drop()
+
+    def fake_run(cmd, check):
+        path = cmd[cmd.index("--save-bed") + 1]
+        np.savez(path, **{f: np.asarray(getattr(want, f)) for f in bench._BED_FIELDS
+                          if getattr(want, f) is not None})
+
+    monkeypatch.setattr(bench.subprocess, "run", fake_run)
+    monkeypatch.setattr(_lib, "_lib", None)
+    got = bench.load_bed(bench.parse_args(["--impl", "reference"]))
+    for f in bench._BED_FIELDS:
+        a, b = getattr(got, f), getattr(want, f)
+        assert (a is None and b is None) or np.array_equal(np.asarray(a), np.asarray(b)), f
+    assert _lib._lib is None

@@ -86,3 +86,29 @@ def test_initialised_particles_step(precision):
     s = E.stats()
     assert s["error_word"] == 0 and s["n_active"] == n
     assert s["n_contacts"] > 0
+
+
+@pytest.mark.parametrize("c", range(5))
+def test_device_constants_match_the_reference_initialiser(c):
+    """Mass, stiffness and damping constant of gdem_init_particles against the
+    reference's own initializeParticles (tests/golden/init_particles.npz, made
+    by the reference harness), bit for bit.  The mass comes back as
+    1 / (1 / m): the engine stores 1 / m."""
+    import os
+    from conftest import GOLDEN
+    from gpudem_gb300 import engine
+    z = dict(np.load(os.path.join(GOLDEN, "init_particles.npz")))
+    r, rho, E, e = (float(a) for a in z["cases"][c])
+    n = 200
+    half = 40 * r
+    lo, hi = np.array([-20 * r, 0.0, -20 * r]), np.array([20 * r, 20 * r, 20 * r])
+    sc = scenes.Scene(x=np.zeros((n, 3)), r=np.full(n, r), m=np.ones(n), k=np.ones(n), eta=np.ones(n), mu=0.5,
+                      dt=1e-6, tris=scenes.box_mesh(half), inlet_lo=lo, inlet_hi=hi)
+    Eng = engine.Engine(sc, precision="fp64", box=(np.full(3, -1.1 * half), np.full(3, 1.1 * half)),
+                        import_scene=False)
+    Eng.init_particles(lo, hi, placement="random", radius=("mono", r), density=rho, youngs_modulus=E,
+                       restitution=e, seed=1)
+    st = Eng.export(history=False)
+    assert np.all(st["k"] == float(z[f"c{c}_k"]))
+    assert np.all(st["etaconst"] == float(z[f"c{c}_etaconst"]))
+    assert np.all(st["m"] == 1.0 / float(z[f"c{c}_invm"]))
