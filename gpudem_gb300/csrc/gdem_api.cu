@@ -315,6 +315,13 @@ struct Impl : EngineBase {
         }
         if (T::mixed) A.add(&v.inv, n);
         A.add(&v.where, n);
+        // cell wall-candidate lists: a count and a base per cell start, and
+        // the shared buffer (4 entries per particle; a cell that finds it
+        // full falls back to the per-particle tree traversal)
+        v.cw_cap = 4 * n + 1024;
+        A.add(&v.cw_cnt, n);
+        A.add(&v.cw_base, n);
+        A.add(&v.cw_list, (size_t)v.cw_cap);
         A.add(&v.rs_hist, (size_t)256 * v.rs_blocks);
         A.add(&v.rs_tot, 256);
         A.add(&v.ctl, 1);
@@ -398,6 +405,7 @@ struct Impl : EngineBase {
         v.seg = M.seg;
         v.segf = M.segf;
         v.seg_tri = M.idx[0];
+        v.tri_aabb = M.aabb_d;
         v.seg_top = M.ntri > 0 ? seg_levels(M.ntri) - 1 : 0;
         for (int L = 0; L < kSegMaxLevels; L++) v.seg_off[L] = L <= v.seg_top ? seg_offset_host(M.ntri, L) : 0;
         if (T::mixed) {
@@ -531,6 +539,10 @@ struct Impl : EngineBase {
         if (2. * rmax + skin > cell)
             return failv(err, GDEM_ERR_ARG, "cell size smaller than the largest list cutoff 2*r_max+skin");
         v.skin = skin;
+        // how far a cell's wall candidates reach: any particle's cutoff
+        // r + skin (mixed rows also widen it by the FP32 error bounds), plus a
+        // margin far above the rounding of a position's cell coordinate
+        v.cw_reach = rmax + skin + (T::mixed ? (double)v.nb_delta + 1e-9 : 0.) + 1e-6 * cell;
         v.thresh_sq = thresh * thresh;
         v.thresh_sqf = (float)v.thresh_sq;
         // inner rows (mixed mode): a tenth of r_max by default, never more than the skin

@@ -109,6 +109,8 @@ struct Ctl {
     unsigned irefresh;        // mixed mode: the inner rows are to be rebuilt
     unsigned pad;
     unsigned long long inner_builds;
+    unsigned wall_alloc;      // entries taken from the cell wall-candidate buffer (this rebuild)
+    unsigned pad2;
 };
 
 template <class T>
@@ -213,6 +215,13 @@ struct View {
     const SegBox* seg;               // mesh tree boxes, level by level
     const SegBoxF* segf;             // mixed mode: the same boxes in FP32
     const int* seg_tri;              // triangle of each level-0 node (Morton order)
+    const double* tri_aabb;          // [6 * ntri] each triangle's box: min xyz, max xyz
+    // wall candidates per occupied cell, indexed by the cell's first sorted
+    // position: every triangle whose box comes within r_max + skin of the
+    // cell, ascending; cw_cnt -1 sends the cell's particles through the tree
+    int *cw_cnt, *cw_base, *cw_list;
+    int cw_cap;                      // capacity of cw_list
+    double cw_reach;                 // r_max + skin (+ the mixed rows' widening) + margin
     int seg_off[kSegMaxLevels];      // first box of each level
     int seg_top;                     // level of the root
     int ntri;

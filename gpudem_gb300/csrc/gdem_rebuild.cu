@@ -358,6 +358,7 @@ template <class T>
 __global__ void k_cells_clear(View<T> v, int gated) {
     const Ctl* ctl = v.ctl;
     if (gated && ctl->refresh == 0u) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) v.ctl->wall_alloc = 0u;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < v.ncells; c += gridDim.x * blockDim.x) {
         v.cell_start[c] = 0;
         v.cell_end[c] = 0;
@@ -420,6 +421,7 @@ __global__ void k_posf(View<T> v, int gated) {
 // banks), and is written out once, mapped back to storage indices through
 // v.where, slot by slot (a warp writes 32 consecutive ints per slot).
 constexpr int kNbBlock = 128;
+constexpr int kNbUnroll = 4;
 
 template <int CAP>
 constexpr size_t nb_smem_bytes() {
@@ -471,27 +473,38 @@ __global__ void __launch_bounds__(kNbBlock) k_neighbors(View<T> v, int gated) {
                         }
                         const int cell = (v.sizey * zz + yy) * v.sizex + xx;
                         const int b = v.cell_start[cell], e = v.cell_end[cell];
-                        for (int q = b; q < e; q++) {
-                            const int j = v.reorder ? q : v.vals[0][q];
-                            if (j == i) continue;
-                            const float4 fj = PF[j];
-                            const float ex = image_dxf(v, fi.x - fj.x), ey = fi.y - fj.y, ez = fi.z - fj.z;
-                            const float dsqf = ex * ex + ey * ey + ez * ez;
-                            const float Rf = rfi + fabsf(fj.w);
-                            const float Rhi = Rf + delta;
-                            if (dsqf > Rhi * Rhi * 1.0000039f) continue;  // (1 + 2^-18): surely outside
-                            const float Rlo = Rf - delta;
-                            bool inside = Rlo > 0.f && dsqf < Rlo * Rlo * 0.9999962f;  // surely inside
-                            if (!inside) {
-                                const double4_32a pj = load_pos(S, j);
-                                const double dx = image_dx(v, xi - pj.x);
-                                const double dy = yi - pj.y;
-                                const double dz = zi - pj.z;
-                                const double distsq = dx * dx + dy * dy + dz * dz;
-                                const double R = ri + pj.w + skin;
-                                inside = distsq < R * R;
+                        // kNbUnroll candidates at a time, their loads in flight together
+                        for (int q0 = b; q0 < e; q0 += kNbUnroll) {
+                            int jj[kNbUnroll];
+                            float4 fj[kNbUnroll];
+#pragma unroll
+                            for (int u = 0; u < kNbUnroll; u++) {
+                                const int q = q0 + u;
+                                jj[u] = q < e ? (v.reorder ? q : v.vals[0][q]) : -1;
+                                if (jj[u] >= 0) fj[u] = PF[jj[u]];
                             }
-                            if (inside) {
+#pragma unroll
+                            for (int u = 0; u < kNbUnroll; u++) {
+                                const int j = jj[u];
+                                if (j < 0 || j == i) continue;
+                                const float ex = image_dxf(v, fi.x - fj[u].x), ey = fi.y - fj[u].y,
+                                            ez = fi.z - fj[u].z;
+                                const float dsqf = ex * ex + ey * ey + ez * ez;
+                                const float Rf = rfi + fabsf(fj[u].w);
+                                const float Rhi = Rf + delta;
+                                if (dsqf > Rhi * Rhi * 1.0000039f) continue;  // (1 + 2^-18): surely outside
+                                const float Rlo = Rf - delta;
+                                bool inside = Rlo > 0.f && dsqf < Rlo * Rlo * 0.9999962f;  // surely inside
+                                if (!inside) {
+                                    const double4_32a pj = load_pos(S, j);
+                                    const double dx = image_dx(v, xi - pj.x);
+                                    const double dy = yi - pj.y;
+                                    const double dz = zi - pj.z;
+                                    const double distsq = dx * dx + dy * dy + dz * dz;
+                                    const double R = ri + pj.w + skin;
+                                    inside = distsq < R * R;
+                                }
+                                if (!inside) continue;
                                 if (count >= CAP) {
                                     overflow = true;
                                     continue;
@@ -556,6 +569,107 @@ __device__ __forceinline__ bool seg_push(unsigned* stack, int& sp, int L, int k,
     stack[sp++] = lv | (unsigned)(2 * k);
     return true;
 }
+// Wall candidates of every occupied cell, one thread per cell (at the
+// cell's first sorted position): the mesh tree traversed with the cell's box
+// grown by v.cw_reach (every particle's cutoff r + skin, the mixed rows'
+// widening, a margin), every triangle whose box overlaps it, ascending.  An
+// ancestor's box contains its leaves', so no overlapping leaf is pruned; a
+// particle's own tree test (sphere against a triangle's box) can pass only
+// for a triangle on its cell's list.  A periodic x also takes the cell's box
+// one period away where it reaches over an x face.  A cell with more than
+// kCellWalls candidates, or one that finds the buffer full, is marked -1 and
+// its particles traverse the tree themselves.
+constexpr int kCellWalls = 96;
+
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_cell_walls(View<T> v, int gated) {
+    Ctl* ctl = v.ctl;
+    if (gated && ctl->refresh == 0u) return;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= v.n) return;
+    const uint32_t* key = v.keys[0];
+    const uint32_t kq = key[q];
+    if (kq == kNoKey || (q > 0 && key[q - 1] == kq)) return;  // not the first particle of a cell
+    const int c[3] = {(int)compact10(kq >> 2), (int)compact10(kq >> 1), (int)compact10(kq)};
+    if (c[0] >= v.sizex || c[1] >= v.sizey || c[2] >= v.sizez || v.ntri == 0) {
+        v.cw_cnt[q] = v.ntri == 0 ? 0 : -1;
+        return;
+    }
+    const double reach = v.cw_reach + (T::mixed ? (double)v.wall_delta : 0.);
+    const double mn[3] = {v.minx, v.miny, v.minz};
+    const double inv[3] = {v.invdx, v.invdy, v.invdz};
+    double lo[3], hi[3];
+    for (int a = 0; a < 3; a++) {
+        lo[a] = mn[a] + (double)(c[a] - 1) / inv[a] - reach;
+        hi[a] = mn[a] + (double)c[a] / inv[a] + reach;
+    }
+    int cand[kCellWalls];
+    int count = 0;
+    bool full = false;
+    unsigned stack[kBvhStack];
+    const int nimg = v.per_x && (hi[0] > v.maxx || lo[0] < v.minx) ? 2 : 1;
+    for (int img = 0; img < nimg && !full; img++) {
+        const double shift = img == 0 ? 0. : (hi[0] > v.maxx ? -v.Lx : v.Lx);
+        const double blo = lo[0] + shift, bhi = hi[0] + shift;
+        int sp = 0;
+        stack[sp++] = (unsigned)v.seg_top << kSegShift;
+        while (sp > 0) {
+            const unsigned e = stack[--sp];
+            const int L = (int)(e >> kSegShift), nk = (int)(e & ((1u << kSegShift) - 1u));
+            const SegBox& B = v.seg[v.seg_off[L] + nk];
+            if (B.lo[0] > bhi || B.hi[0] < blo || B.lo[1] > hi[1] || B.hi[1] < lo[1] || B.lo[2] > hi[2] ||
+                B.hi[2] < lo[2])
+                continue;
+            if (L == 0) {
+                const int t = v.seg_tri[nk];
+                if (count >= kCellWalls) {
+                    full = true;
+                    break;
+                }
+                int k = count;
+                while (k > 0 && cand[k - 1] > t) {
+                    cand[k] = cand[k - 1];
+                    k--;
+                }
+                if (k > 0 && cand[k - 1] == t) {  // met at the other image already
+                    for (int u = k; u < count; u++) cand[u] = cand[u + 1];
+                    continue;
+                }
+                cand[k] = t;
+                count++;
+            } else if (!seg_push(stack, sp, L, nk, v.ntri)) {
+                full = true;
+                break;
+            }
+        }
+    }
+    int base = 0;
+    if (!full && count > 0) {
+        base = (int)atomicAdd(&ctl->wall_alloc, (unsigned)count);
+        if (base + count > v.cw_cap) full = true;
+    }
+    if (full) {
+        v.cw_cnt[q] = -1;
+        return;
+    }
+    for (int k = 0; k < count; k++) v.cw_list[base + k] = cand[k];
+    v.cw_base[q] = base;
+    v.cw_cnt[q] = count;
+}
+
+// The cell wall candidates of particle i's cell (first sorted position q0 and
+// count), or count -1 when its particles traverse the tree themselves.
+template <class T>
+__device__ __forceinline__ int cell_walls_of(const View<T>& v, double x, double y, double z, int& base) {
+    const int cx = cell_x(v, x), cy = cell_coord(y, v.miny, v.invdy), cz = cell_coord(z, v.minz, v.invdz);
+    if (cx < 0 || cx >= v.sizex || cy < 0 || cy >= v.sizey || cz < 0 || cz >= v.sizez) return -1;
+    const int cell = (v.sizey * cz + cy) * v.sizex + cx;
+    if (v.cell_end[cell] <= v.cell_start[cell]) return -1;
+    const int q0 = v.cell_start[cell];
+    base = v.cw_base[q0];
+    return v.cw_cnt[q0];
+}
+
 template <class T, int CAP>
 __global__ void __launch_bounds__(kBlock) k_wall_lists(View<T> v, int gated) {
     Ctl* ctl = v.ctl;
@@ -580,8 +694,32 @@ __global__ void __launch_bounds__(kBlock) k_wall_lists(View<T> v, int gated) {
             const float Rsq = R * R;
             int cand[CAP];
             bool overflow = false;
+            int cbase = 0;
+            const int ccnt = cell_walls_of(v, (double)h.x + (double)l.x, (double)h.y + (double)l.y,
+                                           (double)h.z + (double)l.z, cbase);
+            if (ccnt >= 0) {
+                // the cell's candidates, ascending: the row comes out sorted
+                for (int k = 0; k < ccnt; k++) {
+                    const int t = v.cw_list[cbase + k];
+                    float3 qh = make_float3(h.x, h.y, h.z), ql = pl;
+                    if (v.per_x) {
+                        const float d = qh.x - v.trif[t].v0h[0];
+                        if (d > v.halfLxf || d < -v.halfLxf) {
+                            qh.x = d > 0.f ? qh.x - v.Lxh : qh.x + v.Lxh;
+                            ql.x = 0.f;  // the period's low part is within the margin
+                        }
+                    }
+                    const FeatureF f = closest_feature_f(qh, ql, Rsq, v.trif[t]);
+                    if (!(f.dist < R)) continue;
+                    if (count >= CAP) {
+                        overflow = true;
+                        break;
+                    }
+                    cand[count++] = t;
+                }
+            }
             unsigned stack[kBvhStack];
-            const int nimg = v.per_x && (h.x + R > v.perf[1] || h.x - R < v.perf[0]) ? 2 : 1;
+            const int nimg = ccnt >= 0 ? 0 : (v.per_x && (h.x + R > v.perf[1] || h.x - R < v.perf[0]) ? 2 : 1);
             for (int img = 0; img < nimg; img++) {
                 float3 ph = make_float3(h.x, h.y, h.z);
                 if (img == 1) ph.x = h.x + R > v.perf[1] ? h.x - v.Lxh : h.x + v.Lxh;
@@ -630,11 +768,31 @@ __global__ void __launch_bounds__(kBlock) k_wall_lists(View<T> v, int gated) {
             const double Rsq = R * R;
             int cand[CAP];
             bool overflow = false;
+            int cbase = 0;
+            const int ccnt = cell_walls_of(v, pi.x, py, pz, cbase);
+            if (ccnt >= 0) {
+                // the cell's candidates, ascending, through the same two tests
+                // as the traversal below (sphere against the triangle's box,
+                // then the closest feature): the same row, already sorted
+                for (int k = 0; k < ccnt; k++) {
+                    const int t = v.cw_list[cbase + k];
+                    const double px = image_x_near(v, pi.x, v.tri[t].v0[0]);
+                    const double* bb = v.tri_aabb + 6 * (size_t)t;
+                    if (!sphere_aabb(px, py, pz, Rsq, bb, bb + 3)) continue;
+                    const Feature f = closest_feature(px, py, pz, Rsq, v.tri[t]);
+                    if (!(f.dist < pi.w + v.skin)) continue;
+                    if (count >= CAP) {
+                        overflow = true;
+                        break;
+                    }
+                    cand[count++] = t;
+                }
+            }
             unsigned stack[kBvhStack];
             // periodic x: a sphere within R of an x face also queries the mesh
             // at its image one period away (no triangle is found twice: the
             // mesh's triangles are narrower than a quarter period)
-            const int nimg = v.per_x && (pi.x + R > v.maxx || pi.x - R < v.minx) ? 2 : 1;
+            const int nimg = ccnt >= 0 ? 0 : (v.per_x && (pi.x + R > v.maxx || pi.x - R < v.minx) ? 2 : 1);
             for (int img = 0; img < nimg; img++) {
                 const double px = img == 0 ? pi.x : (pi.x + R > v.maxx ? pi.x - v.Lx : pi.x + v.Lx);
                 int sp = 0;
@@ -698,6 +856,8 @@ __global__ void __launch_bounds__(kBlock) k_wall_lists(View<T> v, int gated) {
 // apart, and it cannot touch before some particle has moved half the inner
 // skin, when the step asks for new rows (ctl->irefresh); every list rebuild
 // asks too.  Gated on that request in every launch mode.
+constexpr int kInnerKeys = 8;
+
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_inner(View<T> v) {
     Ctl* ctl = v.ctl;
@@ -712,24 +872,41 @@ __global__ void __launch_bounds__(kBlock) k_inner(View<T> v) {
             if (hi.w > 0.f) {
                 const int nn = v.nnei[i];
                 const float cut = v.inner_skinf + v.nb_delta;
-                for (int k = 0; k < nn; k++) {
-                    const int j = v.nei[(size_t)k * n + i];
-                    const float4 hj = S.posh[j];
-                    if (!(hj.w > 0.f)) continue;  // inactive for good
-                    const float dx = image_dxf(v, hi.x - hj.x), dy = hi.y - hj.y, dz = hi.z - hj.z;
-                    const float R = hi.w + hj.w + cut;
-                    if (dx * dx + dy * dy + dz * dz < R * R * 1.0000039f) {
+                const bool hints = v.row_mask != 0xFFFFFFFFu;
+                const PBank<T> P = v.P[ctl->p];
+                // the first kInnerKeys history keys in registers for the
+                // slot hints (the rest, rarely used, read when needed)
+                const int nc = hints ? P.nc[i] : 0;
+                int hk[kInnerKeys];
+#pragma unroll
+                for (int q = 0; q < kInnerKeys; q++) hk[q] = q < nc ? P.hid[(size_t)q * n + i] : -1;
+                // four row entries at a time, their gathers in flight together
+                for (int k0 = 0; k0 < nn; k0 += 4) {
+                    int jj[4];
+                    float4 hj[4];
+#pragma unroll
+                    for (int u = 0; u < 4; u++) jj[u] = k0 + u < nn ? v.nei[(size_t)(k0 + u) * n + i] : -1;
+#pragma unroll
+                    for (int u = 0; u < 4; u++)
+                        if (jj[u] >= 0) hj[u] = S.posh[jj[u]];
+#pragma unroll
+                    for (int u = 0; u < 4; u++) {
+                        const int j = jj[u];
+                        if (j < 0 || !(hj[u].w > 0.f)) continue;  // inactive for good
+                        const float dx = image_dxf(v, hi.x - hj[u].x), dy = hi.y - hj[u].y, dz = hi.z - hj[u].z;
+                        const float R = hi.w + hj[u].w + cut;
+                        if (!(dx * dx + dy * dy + dz * dz < R * R * 1.0000039f)) continue;
                         if (m < v.nei_cap) {
                             // the partner's history slot, if it has one, as a hint
                             int e = j;
-                            if (v.row_mask != 0xFFFFFFFFu) {
-                                const PBank<T> P = v.P[ctl->p];
-                                const int nc = P.nc[i];
-                                for (int q = 0; q < nc && q < 63; q++)
-                                    if (P.hid[(size_t)q * n + i] == j) {
-                                        e = j | ((q + 1) << kHintShift);
-                                        break;
-                                    }
+                            if (hints) {
+                                int q = -1;
+#pragma unroll
+                                for (int a = 0; a < kInnerKeys; a++)
+                                    if (q < 0 && hk[a] == j) q = a;
+                                for (int a = kInnerKeys; q < 0 && a < nc && a < 63; a++)
+                                    if (P.hid[(size_t)a * n + i] == j) q = a;
+                                if (q >= 0) e = j | ((q + 1) << kHintShift);
                             }
                             v.inn[(size_t)m * n + i] = e;
                         }
@@ -806,6 +983,7 @@ void launch_rebuild(const View<T>& v, cudaStream_t st, int force) {
         launch_neighbors<T, 64>(v, gated, st);
     else
         launch_neighbors<T, 128>(v, gated, st);
+    k_cell_walls<T><<<g, kBlock, 0, st>>>(v, gated);
     if (v.wall_cap <= 16)
         k_wall_lists<T, 16><<<g, kBlock, 0, st>>>(v, gated);
     else if (v.wall_cap <= 32)

@@ -114,6 +114,12 @@ struct Scene {
     // the published law; the reference has none)
     int model = 0;
     double kn_c = 0., sn_c = 0., kt_c = 0., damp_c = 0., mu_roll = 0.;
+    // Hertz-Mindlin friction and damping per particle (several scenes packed
+    // into one, each with its own material); empty: the scene-wide values.
+    // Particle i's own values enter its contacts, as in the engine.
+    std::vector<double> mu_p, damp_p;
+    double mu_of(int i) const { return mu_p.empty() ? mu : mu_p[i]; }
+    double damp_of(int i) const { return damp_p.empty() ? damp_c : damp_p[i]; }
     std::vector<double> x, v, a, f, w, anga, mom, r, rsq, invr, k, m, sqrtm, invm, moi, invmoi, eta;
     std::vector<int> active, pId;
     std::vector<double> hx, hy, hz, hwx, hwy, hwz;
@@ -551,14 +557,15 @@ bool build_lists(Scene& S) {
 //   kn = 4/3 E* sqrt(R* d), Sn = 2 E* sqrt(R* d), kt = 8 G* sqrt(R* d),
 //   gamma = -2 sqrt(5/6) beta sqrt(S m*), beta = ln e / sqrt(ln^2 e + pi^2).
 // Same operation order as the engine's FP64 kernel.
-void hertz(const Scene& S, double Rstar, double mstar, double delMag, double vdn, V3 n, Contact& c) {
+void hertz(const Scene& S, int i, double Rstar, double mstar, double delMag, double vdn, V3 n, Contact& c) {
+    const double damp = S.damp_of(i);
     const double sqrtRd = sqrt(Rstar * delMag);
     const double fel = S.kn_c * sqrtRd * delMag;
-    const double gn = S.damp_c * sqrt(S.sn_c * sqrtRd * mstar);
+    const double gn = damp * sqrt(S.sn_c * sqrtRd * mstar);
     const double fnm = fel - gn * vdn;
     c.fn = {fnm * n.x, fnm * n.y, fnm * n.z};
     c.kt = S.kt_c * sqrtRd;
-    c.eta = S.damp_c * sqrt(c.kt * mstar);
+    c.eta = damp * sqrt(c.kt * mstar);
     c.Rstar = Rstar;
 }
 
@@ -569,7 +576,7 @@ Contact normal_pp(Scene& S, int i, int j, V3 n, double delMag) {
     const double vdn = dot(vr, n);
     c.vn = scale(vdn, n);
     if (S.model == 1) {
-        hertz(S, S.r[i] * S.r[j] / (S.r[i] + S.r[j]), 1. / (S.invm[i] + S.invm[j]), delMag, vdn, n, c);
+        hertz(S, i, S.r[i] * S.r[j] / (S.r[i] + S.r[j]), 1. / (S.invm[i] + S.invm[j]), delMag, vdn, n, c);
     } else {
         const double meff = 1. / (S.invm[i] + S.invm[j]);
         c.eta = S.eta[i] * sqrt(meff);
@@ -596,7 +603,7 @@ Contact normal_pw(Scene& S, int i, V3 n, double delMag) {
     const double vdn = dot(vr, n);
     c.vn = scale(vdn, n);
     if (S.model == 1) {
-        hertz(S, S.r[i], 1. / S.invm[i], delMag, vdn, n, c);
+        hertz(S, i, S.r[i], 1. / S.invm[i], delMag, vdn, n, c);
     } else {
         c.eta = S.eta[i] * S.sqrtm[i];
         c.kt = S.k[i];
@@ -645,10 +652,11 @@ void tangential(Scene& S, int i, int key, const Contact& c, bool wall, const dou
     V3 ft = scale(-c.kt, dn);
     const double fnsq = dot(c.fn, c.fn);
     const double ftsq = dot(ft, ft);
-    if (ftsq > (S.mu * S.mu) * fnsq) {
+    const double mu = S.mu_of(i);
+    if (ftsq > (mu * mu) * fnsq) {
         if (ftsq != 0.) {
             const V3 t = scale(1. / (sqrt(ftsq) + 1e-15), ft);
-            ft = scale(S.mu * sqrt(fnsq), t);
+            ft = scale(mu * sqrt(fnsq), t);
             dn = scale(-1. / c.kt, ft);
         } else {
             ft = {0., 0., 0.};
@@ -902,6 +910,22 @@ void* orc_create(int N, const double* x, const double* v, const double* w, const
 }
 
 void orc_destroy(void* h) { delete (Scene*)h; }
+
+// Hertz-Mindlin friction and restitution per particle, the damping factor
+// -2 sqrt(5/6) beta from each restitution as the engine's
+// gdem_set_particle_materials computes it.  Returns -1 for the linear law.
+int orc_set_materials(void* h, const double* mu, const double* e) {
+    Scene& S = *(Scene*)h;
+    if (S.model != 1) return -1;
+    S.mu_p.assign(mu, mu + S.N);
+    S.damp_p.resize(S.N);
+    for (int i = 0; i < S.N; i++) {
+        const double le = log(e[i]);
+        const double beta = le / sqrt(le * le + M_PI * M_PI);
+        S.damp_p[i] = -2. * sqrt(5. / 6.) * beta;
+    }
+    return 0;
+}
 
 int orc_step(void* h, int nsteps) {
     Scene* S = (Scene*)h;

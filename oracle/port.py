@@ -29,6 +29,8 @@ def lib():
                                  vp, C.c_int, vp, vp, C.c_double, C.c_double, C.c_int, C.c_double, C.c_double,
                                  C.c_double, C.c_double, C.c_int]
         L.orc_destroy.argtypes = [vp]
+        L.orc_set_materials.argtypes = [vp, vp, vp]
+        L.orc_set_materials.restype = C.c_int
         L.orc_step.argtypes = [vp, C.c_int]
         L.orc_step.restype = C.c_int
         L.orc_rebuild.argtypes = [vp]
@@ -89,6 +91,14 @@ class OracleScene:
                               float(sc.nu), float(sc.e), float(sc.mu_roll), 1 if sc.periodic_x else 0)
         if not self.h:
             raise ValueError("oracle: bad scene (a periodic x needs at least 3 cells across the period)")
+        if sc.mu_p is not None:
+            # per-particle friction and restitution (packed scenes), as the
+            # engine takes them through gdem_set_particle_materials
+            mu_p = np.ascontiguousarray(sc.mu_p, np.float64)
+            e_p = np.ascontiguousarray(sc.e_p, np.float64)
+            self._keep += [mu_p, e_p]
+            if L.orc_set_materials(self.h, _vp(mu_p), _vp(e_p)) != 0:
+                raise ValueError("oracle: per-particle materials need the Hertz-Mindlin law")
 
     def step(self, n=1):
         rc = lib().orc_step(self.h, int(n))

@@ -130,10 +130,10 @@ def test_snapshot_with_a_corrupt_history_key_is_refused(tmp_path, precision):
     exactly as an engine that never saw the file."""
     import struct
     from gpudem_gb300 import _lib, engine, scenes
-    sc = scenes.config3_helical_chute(n=5_000, n_tri=2_000, v_sigma=0.5)
+    sc = scenes.config3_helical_chute(n=20_000, n_tri=5_000, v_sigma=0.5)
     path = str(tmp_path / "snap.bin")
     A = engine.Engine(sc, precision=precision, model="hertz_mindlin")
-    A.step(200)
+    A.step(900)
     A.save_snapshot(path)
     assert _lib.load().gdem_check_snapshot(path.encode(), A.ntri) == 0
     raw = bytearray(open(path, "rb").read())
