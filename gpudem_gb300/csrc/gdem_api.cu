@@ -260,6 +260,10 @@ struct Impl : EngineBase {
         v.occupancy = d.occupancy > 0 ? d.occupancy : 0;
         // failure-detection tests only: fewer tries for the step kernels'
         // pipeline waits, so that a wait gives up and reports GDEM_EW_TIMEOUT
+        {
+            const char* nb = getenv("GDEM_NEIGHBORS");
+            v.nb_thread = nb && strcmp(nb, "thread") == 0 ? 1 : 0;
+        }
         v.wait_tries = kSpinLimit;
         if (const char* wt = getenv("GDEM_TEST_WAIT_TRIES")) v.wait_tries = (unsigned)strtoul(wt, nullptr, 10);
         v.reorder = d.reorder == 0 ? 0 : 1;
@@ -322,6 +326,7 @@ struct Impl : EngineBase {
         A.add(&v.cw_cnt, n);
         A.add(&v.cw_base, n);
         A.add(&v.cw_list, (size_t)v.cw_cap);
+        A.add(&v.cell_list, n);
         A.add(&v.rs_hist, (size_t)256 * v.rs_blocks);
         A.add(&v.rs_tot, 256);
         A.add(&v.ctl, 1);

@@ -110,7 +110,7 @@ struct Ctl {
     unsigned pad;
     unsigned long long inner_builds;
     unsigned wall_alloc;      // entries taken from the cell wall-candidate buffer (this rebuild)
-    unsigned pad2;
+    unsigned ncell_list;      // occupied cells listed in cell_list (this rebuild)
 };
 
 template <class T>
@@ -220,6 +220,7 @@ struct View {
     // position: every triangle whose box comes within r_max + skin of the
     // cell, ascending; cw_cnt -1 sends the cell's particles through the tree
     int *cw_cnt, *cw_base, *cw_list;
+    int* cell_list;                  // first sorted position of every occupied cell (any order)
     int cw_cap;                      // capacity of cw_list
     double cw_reach;                 // r_max + skin (+ the mixed rows' widening) + margin
     int seg_off[kSegMaxLevels];      // first box of each level
@@ -243,6 +244,8 @@ struct View {
     int per_particle_mat;            // Hertz-Mindlin: mu and damping from mat.x, mat.y of each particle
     int kernel_variant;              // mixed step kernel: 0 default, 1 cooperative, 2 staged, 3 one-pass
     int occupancy;                   // mixed step kernel: resident CTAs per SM to size for (0 default)
+    int nb_thread;                   // mixed mode: Verlet rows by the thread-per-particle scan
+                                     // (GDEM_NEIGHBORS=thread) instead of a warp per cell
     unsigned wait_tries;             // mixed step kernels: tries of each pipeline wait on a bulk copy
                                      // (kSpinLimit; GDEM_TEST_WAIT_TRIES lowers it to test the timeout path)
     // the scalars above rounded to FP32 once, for the mixed step
