@@ -309,10 +309,11 @@ def run_engine(args):
         # one step kernel per step (+ the mesh tree rebuild: keys, 4 sort
         # passes, tree) + the kernels of each list rebuild (keys, 4 sort passes,
         # reorder (+ its inverse order in mixed mode), cell clear, cell ranges,
-        # Verlet (+ the FP32 position copy in FP64 mode), walls) + each
+        # the occupied-cell list (count, scan, emit), Verlet (+ the FP32
+        # position copy in FP64 mode), cell wall candidates, walls) + each
         # inner-row build
         "gpu_launches": args.steps * (1 + (0 if args.bvh_once else 2 + sort_launches(int(sc.tris.shape[0]))))
-                        + reb * (7 + sort_launches(sc.n))
+                        + reb * (11 + sort_launches(sc.n))
                         + int(st1["inner_builds"] - st0["inner_builds"]),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
@@ -580,7 +581,7 @@ def run_batched(args):
                       "one_by_one_value": seq_value, "one_by_one_steps_per_scene": seq_steps,
                       "batched_over_one_by_one": value / seq_value, "rebuilds_in_timed_region": reb},
            "clocks": clk.summary(),
-           "gpu_launches": args.steps + reb * (7 + sort_launches(packed.n))
+           "gpu_launches": args.steps + reb * (11 + sort_launches(packed.n))
                            + int(st1["inner_builds"] - st0["inner_builds"])}
     print(json.dumps(out))
 

@@ -327,6 +327,7 @@ struct Impl : EngineBase {
         A.add(&v.cw_base, n);
         A.add(&v.cw_list, (size_t)v.cw_cap);
         A.add(&v.cell_list, n);
+        A.add(&v.cell_bc, (size_t)(n + kBlock - 1) / kBlock + 1);
         A.add(&v.rs_hist, (size_t)256 * v.rs_blocks);
         A.add(&v.rs_tot, 256);
         A.add(&v.ctl, 1);

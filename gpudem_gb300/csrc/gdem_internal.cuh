@@ -220,7 +220,8 @@ struct View {
     // position: every triangle whose box comes within r_max + skin of the
     // cell, ascending; cw_cnt -1 sends the cell's particles through the tree
     int *cw_cnt, *cw_base, *cw_list;
-    int* cell_list;                  // first sorted position of every occupied cell (any order)
+    int* cell_list;                  // first sorted position of every occupied cell, ascending
+    int* cell_bc;                    // [blocks of kBlock sorted positions + 1] cell starts per block, scanned
     int cw_cap;                      // capacity of cw_list
     double cw_reach;                 // r_max + skin (+ the mixed rows' widening) + margin
     int seg_off[kSegMaxLevels];      // first box of each level

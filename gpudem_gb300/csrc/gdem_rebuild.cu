@@ -358,10 +358,7 @@ template <class T>
 __global__ void k_cells_clear(View<T> v, int gated) {
     const Ctl* ctl = v.ctl;
     if (gated && ctl->refresh == 0u) return;
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        v.ctl->wall_alloc = 0u;
-        v.ctl->ncell_list = 0u;
-    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) v.ctl->wall_alloc = 0u;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < v.ncells; c += gridDim.x * blockDim.x) {
         v.cell_start[c] = 0;
         v.cell_end[c] = 0;
@@ -394,11 +391,74 @@ __global__ void k_cell_ranges(View<T> v, int gated) {
         return;
     }
     const int cell = (v.sizey * cz + cy) * v.sizex + cx;
-    if (q == 0 || key[q - 1] != kq) {
-        v.cell_start[cell] = q;
-        v.cell_list[atomicAdd(&v.ctl->ncell_list, 1u)] = q;  // the occupied cells, in any order
-    }
+    if (q == 0 || key[q - 1] != kq) v.cell_start[cell] = q;
     if (q == n - 1 || key[q + 1] != kq) v.cell_end[cell] = q + 1;
+}
+
+// The occupied cells in sorted (Morton) order: the first sorted position of
+// every cell inside the grid, compacted by a count per block of kBlock
+// positions, one exclusive scan over the blocks and an emit that ranks each
+// start within its block.  Neighbouring entries are neighbouring cells, so
+// the per-cell kernels that walk the list stay coherent.
+template <class T>
+__device__ __forceinline__ bool is_cell_start(const View<T>& v, int q) {
+    if (q >= v.n) return false;
+    const uint32_t* key = v.keys[0];
+    const uint32_t kq = key[q];
+    if (kq == kNoKey || (q > 0 && key[q - 1] == kq)) return false;
+    return (int)compact10(kq >> 2) < v.sizex && (int)compact10(kq >> 1) < v.sizey && (int)compact10(kq) < v.sizez;
+}
+
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_cell_count(View<T> v, int gated) {
+    if (gated && v.ctl->refresh == 0u) return;
+    const int c = __syncthreads_count(is_cell_start(v, blockIdx.x * blockDim.x + threadIdx.x));
+    if (threadIdx.x == 0) v.cell_bc[blockIdx.x] = c;
+}
+
+// Exclusive scan of the nb block counts in place, by one CTA of 1024 threads
+// (each a run of consecutive counts); the total goes to ctl->ncell_list.
+template <class T>
+__global__ void __launch_bounds__(1024) k_cell_scan(View<T> v, int gated, int nb) {
+    if (gated && v.ctl->refresh == 0u) return;
+    __shared__ int part[1024];
+    const int t = threadIdx.x;
+    const int per = (nb + 1023) / 1024;
+    const int lo = t * per, hi = min(lo + per, nb);
+    int sum = 0;
+    for (int b = lo; b < hi; b++) sum += v.cell_bc[b];
+    part[t] = sum;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        const int add = t >= o ? part[t - o] : 0;
+        __syncthreads();
+        part[t] += add;
+        __syncthreads();
+    }
+    int run = part[t] - sum;  // exclusive prefix of this run
+    for (int b = lo; b < hi; b++) {
+        const int c = v.cell_bc[b];
+        v.cell_bc[b] = run;
+        run += c;
+    }
+    if (t == 1023) v.ctl->ncell_list = (unsigned)part[1023];
+}
+
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_cell_emit(View<T> v, int gated) {
+    if (gated && v.ctl->refresh == 0u) return;
+    __shared__ int wbase[kBlock / 32];
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool f = is_cell_start(v, q);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned m = __ballot_sync(0xffffffffu, f);
+    if (lane == 0) wbase[w] = __popc(m);
+    __syncthreads();
+    if (f) {
+        int off = v.cell_bc[blockIdx.x];
+        for (int u = 0; u < w; u++) off += wbase[u];
+        v.cell_list[off + __popc(m & ((1u << lane) - 1u))] = q;
+    }
 }
 
 // ===================================================================== Verlet lists
@@ -575,7 +635,8 @@ constexpr int kNwStage = 512;   // staged candidates per warp
 
 template <int CAP>
 constexpr size_t nw_smem_bytes() {
-    return (sizeof(float4) + sizeof(int)) * (size_t)kNwWarps * kNwStage + 2 * sizeof(int) * (size_t)kNwWarps * CAP;
+    return (sizeof(float4) + 2 * sizeof(int)) * (size_t)kNwWarps * kNwStage +
+           2 * sizeof(int) * (size_t)kNwWarps * CAP;
 }
 
 // Bitonic sort of 32 M (key, value) pairs held M per lane (element m * 32 +
@@ -644,7 +705,8 @@ __global__ void __launch_bounds__(kNwWarps * 32) k_neighbors_warp(View<Mixed> v,
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float4* sp = reinterpret_cast<float4*>(nw_raw) + (size_t)warp * kNwStage;
     int* sj = reinterpret_cast<int*>(nw_raw + sizeof(float4) * kNwWarps * kNwStage) + (size_t)warp * kNwStage;
-    int* rowj = reinterpret_cast<int*>(nw_raw + (sizeof(float4) + sizeof(int)) * kNwWarps * kNwStage) +
+    int* spid = sj + (size_t)kNwWarps * kNwStage;
+    int* rowj = reinterpret_cast<int*>(nw_raw + (sizeof(float4) + 2 * sizeof(int)) * kNwWarps * kNwStage) +
                 (size_t)warp * 2 * CAP;
     int* rowp = rowj + CAP;
     const int n = v.n;
@@ -706,15 +768,19 @@ __global__ void __launch_bounds__(kNwWarps * 32) k_neighbors_warp(View<Mixed> v,
                     const int j = v.reorder ? q : v.vals[0][q];
                     sj[idx] = j;
                     sp[idx] = PF[j];
+                    spid[idx] = pidv[j];
                 }
             }
             __syncwarp();
         };
         const bool one_stage = T <= kNwStage;
         if (one_stage) stage(0, T);
+        // the cell itself is neighbour 13 (offset 0, 0, 0): its particles are
+        // staged in sorted order from position e13
+        const int e13 = __shfl_sync(0xffffffffu, excl, 13);
         for (int qp = q0; qp < qe; qp++) {
             const int i = v.reorder ? qp : v.vals[0][qp];
-            const float4 fi = PF[i];
+            const float4 fi = one_stage ? sp[e13 + (qp - q0)] : PF[i];
             const float rfi = fabsf(fi.w) + skinf;
             int count = 0;
             for (int seg = 0; seg < T; seg += kNwStage) {
@@ -753,15 +819,16 @@ __global__ void __launch_bounds__(kNwWarps * 32) k_neighbors_warp(View<Mixed> v,
                     const unsigned msk = __ballot_sync(0xffffffffu, hit);
                     if (hit) {
                         const int pos = count + __popc(msk & lt);
-                        if (pos < CAP) rowj[pos] = j;
+                        if (pos < CAP) {
+                            rowj[pos] = j;
+                            rowp[pos] = spid[idx];
+                        }
                     }
                     count += __popc(msk);
                 }
             }
             __syncwarp();
             const int cs = count < CAP ? count : CAP;
-            for (int e = lane; e < cs; e += 32) rowp[e] = pidv[rowj[e]];
-            __syncwarp();
             if (count > CAP || count > v.nei_cap) err |= 0x1u;
             const int mrow = count < v.nei_cap ? count : v.nei_cap;
             if (cs <= 32)
@@ -1230,6 +1297,9 @@ void launch_rebuild(const View<T>& v, cudaStream_t st, int force) {
     const int gc = grid_for(v.ncells) < 4096 ? grid_for(v.ncells) : 4096;
     k_cells_clear<T><<<gc, kBlock, 0, st>>>(v, gated);
     k_cell_ranges<T><<<g, kBlock, 0, st>>>(v, gated);
+    k_cell_count<T><<<g, kBlock, 0, st>>>(v, gated);
+    k_cell_scan<T><<<1, 1024, 0, st>>>(v, gated, g);
+    k_cell_emit<T><<<g, kBlock, 0, st>>>(v, gated);
     if constexpr (!T::mixed) k_posf<T><<<g, kBlock, 0, st>>>(v, gated);
     // mixed mode: a warp per occupied cell (v.nb_thread: the thread-per-particle
     // scan, for comparison); FP64 mode: a thread per particle
