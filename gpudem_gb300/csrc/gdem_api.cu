@@ -260,10 +260,6 @@ struct Impl : EngineBase {
         v.occupancy = d.occupancy > 0 ? d.occupancy : 0;
         // failure-detection tests only: fewer tries for the step kernels'
         // pipeline waits, so that a wait gives up and reports GDEM_EW_TIMEOUT
-        {
-            const char* nb = getenv("GDEM_NEIGHBORS");
-            v.nb_thread = nb && strcmp(nb, "thread") == 0 ? 1 : 0;
-        }
         v.wait_tries = kSpinLimit;
         if (const char* wt = getenv("GDEM_TEST_WAIT_TRIES")) v.wait_tries = (unsigned)strtoul(wt, nullptr, 10);
         v.reorder = d.reorder == 0 ? 0 : 1;

@@ -221,6 +221,7 @@ struct View {
     // cell, ascending; cw_cnt -1 sends the cell's particles through the tree
     int *cw_cnt, *cw_base, *cw_list;
     int* cell_list;                  // first sorted position of every occupied cell, ascending
+                                     // (the cells the wall candidates are found for)
     int* cell_bc;                    // [blocks of kBlock sorted positions + 1] cell starts per block, scanned
     int cw_cap;                      // capacity of cw_list
     double cw_reach;                 // r_max + skin (+ the mixed rows' widening) + margin
@@ -245,8 +246,6 @@ struct View {
     int per_particle_mat;            // Hertz-Mindlin: mu and damping from mat.x, mat.y of each particle
     int kernel_variant;              // mixed step kernel: 0 default, 1 cooperative, 2 staged, 3 one-pass
     int occupancy;                   // mixed step kernel: resident CTAs per SM to size for (0 default)
-    int nb_thread;                   // mixed mode: Verlet rows by the thread-per-particle scan
-                                     // (GDEM_NEIGHBORS=thread) instead of a warp per cell
     unsigned wait_tries;             // mixed step kernels: tries of each pipeline wait on a bulk copy
                                      // (kSpinLimit; GDEM_TEST_WAIT_TRIES lowers it to test the timeout path)
     // the scalars above rounded to FP32 once, for the mixed step

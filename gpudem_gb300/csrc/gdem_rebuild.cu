@@ -399,7 +399,8 @@ __global__ void k_cell_ranges(View<T> v, int gated) {
 // every cell inside the grid, compacted by a count per block of kBlock
 // positions, one exclusive scan over the blocks and an emit that ranks each
 // start within its block.  Neighbouring entries are neighbouring cells, so
-// the per-cell kernels that walk the list stay coherent.
+// the wall-candidate traversals of neighbouring threads (k_cell_walls) walk
+// much the same part of the mesh tree.
 template <class T>
 __device__ __forceinline__ bool is_cell_start(const View<T>& v, int q) {
     if (q >= v.n) return false;
@@ -620,252 +621,6 @@ static void launch_neighbors(const View<T>& v, int gated, cudaStream_t st) {
         configured = true;
     }
     k_neighbors<T, CAP><<<(v.n + kNbBlock - 1) / kNbBlock, kNbBlock, nb_smem_bytes<CAP>(), st>>>(v, gated);
-}
-
-// Mixed mode: a warp per occupied cell.  The particles of a cell share the
-// 27 neighbour cells, so the warp stages their candidates once (storage index
-// and high-part position, in shared memory) and then, particle by particle,
-// tests 32 candidates at a time with every lane busy: the same FP32
-// prefilter and FP64 test near the cutoff as k_neighbors, the hits compacted
-// by ballot into the row, the row sorted by partner pId with a bitonic sort
-// across the warp, and written out.  A neighbourhood larger than the stage
-// is staged in segments, again for every particle of the cell.
-constexpr int kNwWarps = 4;     // warps per CTA
-constexpr int kNwStage = 512;   // staged candidates per warp
-
-template <int CAP>
-constexpr size_t nw_smem_bytes() {
-    return (sizeof(float4) + 2 * sizeof(int)) * (size_t)kNwWarps * kNwStage +
-           2 * sizeof(int) * (size_t)kNwWarps * CAP;
-}
-
-// Bitonic sort of 32 M (key, value) pairs held M per lane (element m * 32 +
-// lane in register m), ascending by key; keys are distinct except padding.
-template <int M>
-__device__ __forceinline__ void warp_bitonic(int (&key)[M], int (&val)[M], int lane) {
-    constexpr int N = 32 * M;
-#pragma unroll
-    for (int k = 2; k <= N; k <<= 1) {
-#pragma unroll
-        for (int j = k >> 1; j > 0; j >>= 1) {
-#pragma unroll
-            for (int m = 0; m < M; m++) {
-                const bool up = ((m * 32 + lane) & k) == 0;
-                if (j >= 32) {
-                    const int pm = m ^ (j >> 5);
-                    if (pm > m) {
-                        const bool sw = up ? (key[m] > key[pm]) : (key[m] < key[pm]);
-                        if (sw) {
-                            const int tk = key[m], tv = val[m];
-                            key[m] = key[pm];
-                            val[m] = val[pm];
-                            key[pm] = tk;
-                            val[pm] = tv;
-                        }
-                    }
-                } else {
-                    const int ok = __shfl_xor_sync(0xffffffffu, key[m], j);
-                    const int ov = __shfl_xor_sync(0xffffffffu, val[m], j);
-                    const bool lower = (lane & j) == 0;
-                    if (lower == up ? (ok < key[m]) : (ok > key[m])) {
-                        key[m] = ok;
-                        val[m] = ov;
-                    }
-                }
-            }
-        }
-    }
-}
-
-// Sort the first cs entries of (rowp, rowj) by rowp across the warp and
-// write the first mrow of them, as storage indices, into particle i's row.
-template <int M>
-__device__ __forceinline__ void nw_sort_write(const int* rowp, const int* rowj, int cs, int mrow, int* nei, int n,
-                                              int i, int lane) {
-    int key[M], val[M];
-#pragma unroll
-    for (int m = 0; m < M; m++) {
-        const int e = m * 32 + lane;
-        key[m] = e < cs ? rowp[e] : 0x7fffffff;
-        val[m] = e < cs ? rowj[e] : -1;
-    }
-    warp_bitonic<M>(key, val, lane);
-#pragma unroll
-    for (int m = 0; m < M; m++) {
-        const int e = m * 32 + lane;
-        if (e < mrow) nei[(size_t)e * n + i] = val[m];
-    }
-}
-
-template <int CAP>
-__global__ void __launch_bounds__(kNwWarps * 32) k_neighbors_warp(View<Mixed> v, int gated) {
-    extern __shared__ __align__(16) unsigned char nw_raw[];
-    Ctl* ctl = v.ctl;
-    if (gated && ctl->refresh == 0u) return;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    float4* sp = reinterpret_cast<float4*>(nw_raw) + (size_t)warp * kNwStage;
-    int* sj = reinterpret_cast<int*>(nw_raw + sizeof(float4) * kNwWarps * kNwStage) + (size_t)warp * kNwStage;
-    int* spid = sj + (size_t)kNwWarps * kNwStage;
-    int* rowj = reinterpret_cast<int*>(nw_raw + (sizeof(float4) + 2 * sizeof(int)) * kNwWarps * kNwStage) +
-                (size_t)warp * 2 * CAP;
-    int* rowp = rowj + CAP;
-    const int n = v.n;
-    const SBank<Mixed> S = v.S[ctl->s];
-    const int* __restrict__ pidv = v.P[ctl->p].pid;
-    const float4* __restrict__ PF = S.posh;
-    const int ncl = (int)ctl->ncell_list;
-    const float skinf = (float)v.skin, delta = v.nb_delta;
-    const double skin = v.skin;
-    const unsigned lt = (1u << lane) - 1u;
-    int wmax = 0;
-    unsigned err = 0u;
-    for (int ci = blockIdx.x * kNwWarps + warp; ci < ncl; ci += gridDim.x * kNwWarps) {
-        const int q0 = v.cell_list[ci];
-        const uint32_t kq = v.keys[0][q0];
-        const int cx = (int)compact10(kq >> 2), cy = (int)compact10(kq >> 1), cz = (int)compact10(kq);
-        const int qe = v.cell_end[(v.sizey * cz + cy) * v.sizex + cx];
-        // neighbour cell of lane k < 27 (offsets x fastest, then y, then z);
-        // cells outside the grid hold nobody, a periodic x wraps
-        int b = 0, cnt = 0;
-        if (lane < 27) {
-            int xx = cx + lane % 3 - 1;
-            const int yy = cy + (lane / 3) % 3 - 1, zz = cz + lane / 9 - 1;
-            bool ok = yy >= 0 && yy < v.sizey && zz >= 0 && zz < v.sizez;
-            if (v.per_x) {
-                if (xx < 1) xx += v.nxp;
-                else if (xx > v.nxp) xx -= v.nxp;
-            } else {
-                ok = ok && xx >= 0 && xx < v.sizex;
-            }
-            if (ok) {
-                const int cc = (v.sizey * zz + yy) * v.sizex + xx;
-                b = v.cell_start[cc];
-                cnt = v.cell_end[cc] - b;
-            }
-        }
-        int excl = cnt;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int y = __shfl_up_sync(0xffffffffu, excl, o);
-            if (lane >= o) excl += y;
-        }
-        const int T = __shfl_sync(0xffffffffu, excl, 31);
-        excl -= cnt;
-        // stage candidates [seg, seg + segn) of the concatenated neighbour cells
-        auto stage = [&](int seg, int segn) {
-            for (int base = 0; base < segn; base += 32) {
-                const int idx = base + lane;
-                const int g = seg + (idx < segn ? idx : segn - 1);
-                int k = 0;
-#pragma unroll
-                for (int step = 16; step > 0; step >>= 1) {
-                    const int e2 = __shfl_sync(0xffffffffu, excl, min(k + step, 31));
-                    if (k + step < 27 && e2 <= g) k += step;
-                }
-                const int bk = __shfl_sync(0xffffffffu, b, k), ek = __shfl_sync(0xffffffffu, excl, k);
-                if (idx < segn) {
-                    const int q = bk + (g - ek);
-                    const int j = v.reorder ? q : v.vals[0][q];
-                    sj[idx] = j;
-                    sp[idx] = PF[j];
-                    spid[idx] = pidv[j];
-                }
-            }
-            __syncwarp();
-        };
-        const bool one_stage = T <= kNwStage;
-        if (one_stage) stage(0, T);
-        // the cell itself is neighbour 13 (offset 0, 0, 0): its particles are
-        // staged in sorted order from position e13
-        const int e13 = __shfl_sync(0xffffffffu, excl, 13);
-        for (int qp = q0; qp < qe; qp++) {
-            const int i = v.reorder ? qp : v.vals[0][qp];
-            const float4 fi = one_stage ? sp[e13 + (qp - q0)] : PF[i];
-            const float rfi = fabsf(fi.w) + skinf;
-            int count = 0;
-            for (int seg = 0; seg < T; seg += kNwStage) {
-                const int segn = min(kNwStage, T - seg);
-                if (!one_stage) {
-                    __syncwarp();
-                    stage(seg, segn);
-                }
-                for (int c0 = 0; c0 < segn; c0 += 32) {
-                    const int idx = c0 + lane;
-                    bool hit = false;
-                    int j = -1;
-                    if (idx < segn) {
-                        j = sj[idx];
-                        if (j != i) {
-                            const float4 fj = sp[idx];
-                            const float ex = image_dxf(v, fi.x - fj.x), ey = fi.y - fj.y, ez = fi.z - fj.z;
-                            const float dsqf = ex * ex + ey * ey + ez * ez;
-                            const float Rf = rfi + fabsf(fj.w);
-                            const float Rhi = Rf + delta;
-                            if (!(dsqf > Rhi * Rhi * 1.0000039f)) {  // (1 + 2^-18): not surely outside
-                                const float Rlo = Rf - delta;
-                                hit = Rlo > 0.f && dsqf < Rlo * Rlo * 0.9999962f;  // surely inside
-                                if (!hit) {
-                                    const double4_32a pi = load_pos(S, i);
-                                    const double4_32a pj = load_pos(S, j);
-                                    const double dx = image_dx(v, pi.x - pj.x);
-                                    const double dy = pi.y - pj.y;
-                                    const double dz = pi.z - pj.z;
-                                    const double R = pi.w + pj.w + skin;
-                                    hit = dx * dx + dy * dy + dz * dz < R * R;
-                                }
-                            }
-                        }
-                    }
-                    const unsigned msk = __ballot_sync(0xffffffffu, hit);
-                    if (hit) {
-                        const int pos = count + __popc(msk & lt);
-                        if (pos < CAP) {
-                            rowj[pos] = j;
-                            rowp[pos] = spid[idx];
-                        }
-                    }
-                    count += __popc(msk);
-                }
-            }
-            __syncwarp();
-            const int cs = count < CAP ? count : CAP;
-            if (count > CAP || count > v.nei_cap) err |= 0x1u;
-            const int mrow = count < v.nei_cap ? count : v.nei_cap;
-            if (cs <= 32)
-                nw_sort_write<1>(rowp, rowj, cs, mrow, v.nei, n, i, lane);
-            else if (CAP >= 64 && cs <= 64)
-                nw_sort_write<(CAP >= 64 ? 2 : 1)>(rowp, rowj, cs, mrow, v.nei, n, i, lane);
-            else
-                nw_sort_write<CAP / 32>(rowp, rowj, cs, mrow, v.nei, n, i, lane);
-            if (lane == 0) {
-                v.nnei[i] = mrow;
-                v.refh[i] = make_float4(fi.x, fi.y, fi.z, 0.f);
-            }
-            wmax = max(wmax, count);
-            __syncwarp();
-        }
-        __syncwarp();
-    }
-    if (lane == 0) {
-        if (err) atomicOr(&ctl->error, err);
-        if (wmax > 0) atomicMax(&ctl->max_nei, wmax);
-    }
-}
-
-template <int CAP>
-static void launch_neighbors_warp(const View<Mixed>& v, int gated, cudaStream_t st) {
-    static int grid = 0;
-    if (!grid) {
-        cudaFuncSetAttribute(k_neighbors_warp<CAP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)nw_smem_bytes<CAP>());
-        int per_sm = 0, dev = 0, sms = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_neighbors_warp<CAP>, kNwWarps * 32,
-                                                      nw_smem_bytes<CAP>());
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        grid = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
-    }
-    k_neighbors_warp<CAP><<<grid, kNwWarps * 32, nw_smem_bytes<CAP>(), st>>>(v, gated);
 }
 
 // ===================================================================== wall lists
@@ -1301,27 +1056,12 @@ void launch_rebuild(const View<T>& v, cudaStream_t st, int force) {
     k_cell_scan<T><<<1, 1024, 0, st>>>(v, gated, g);
     k_cell_emit<T><<<g, kBlock, 0, st>>>(v, gated);
     if constexpr (!T::mixed) k_posf<T><<<g, kBlock, 0, st>>>(v, gated);
-    // mixed mode: a warp per occupied cell (v.nb_thread: the thread-per-particle
-    // scan, for comparison); FP64 mode: a thread per particle
-    const bool nb_thread = v.nb_thread != 0;
-    if constexpr (T::mixed) {
-        if (!nb_thread) {
-            if (v.nei_cap <= 32)
-                launch_neighbors_warp<32>(v, gated, st);
-            else if (v.nei_cap <= 64)
-                launch_neighbors_warp<64>(v, gated, st);
-            else
-                launch_neighbors_warp<128>(v, gated, st);
-        }
-    }
-    if (!T::mixed || nb_thread) {
-        if (v.nei_cap <= 32)
-            launch_neighbors<T, 32>(v, gated, st);
-        else if (v.nei_cap <= 64)
-            launch_neighbors<T, 64>(v, gated, st);
-        else
-            launch_neighbors<T, 128>(v, gated, st);
-    }
+    if (v.nei_cap <= 32)
+        launch_neighbors<T, 32>(v, gated, st);
+    else if (v.nei_cap <= 64)
+        launch_neighbors<T, 64>(v, gated, st);
+    else
+        launch_neighbors<T, 128>(v, gated, st);
     k_cell_walls<T><<<g, kBlock, 0, st>>>(v, gated);
     if (v.wall_cap <= 16)
         k_wall_lists<T, 16><<<g, kBlock, 0, st>>>(v, gated);

@@ -79,25 +79,3 @@ def test_wall_lists_large_mesh(precision):
             E.rebuild()
     E.close()
 
-
-@pytest.mark.parametrize("reorder", [True, False])
-def test_mixed_verlet_rows_by_cell_warps_match_the_thread_scan(monkeypatch, reorder):
-    """Mixed-mode Verlet rows from a warp per occupied cell (the default) and
-    from the thread-per-particle scan (GDEM_NEIGHBORS=thread) are the same
-    rows, over a pour with rebuilds, with and without reordering."""
-    from dataclasses import replace
-    from gpudem_gb300 import engine, scenes
-    sc = replace(scenes.config3_chute_pour(n=60_000, n_tri=8_000), dt=2e-5, e=0.1)
-    kw = dict(precision="mixed", model="hertz_mindlin", reorder=reorder)
-    monkeypatch.setenv("GDEM_NEIGHBORS", "thread")
-    A = engine.Engine(sc, **kw)
-    monkeypatch.delenv("GDEM_NEIGHBORS")
-    B = engine.Engine(sc, **kw)
-    for E in (A, B):
-        E.step(300)
-    la, lb = A.lists(), B.lists()
-    for a, b in zip(la, lb):
-        assert np.array_equal(a, b)
-    sa, sb = A.stats(), B.stats()
-    assert sa["rebuilds"] == sb["rebuilds"] > 3 and sa["error_word"] == sb["error_word"] == 0
-    assert np.array_equal(A.export(history=True)["x"], B.export(history=True)["x"])
