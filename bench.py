@@ -256,13 +256,18 @@ def run_engine(args):
     peak, peak_kind = _peaks()
     achieved = bytes_launch / (k_ms / 1e3) / 1e9
     traffic = args.traffic
+    traffic_source = "--traffic" if traffic is not None else None
     if traffic is None and mixed and args.workload == "poured" and args.n == 1_000_000 and args.model == "hertz_mindlin":
         # dram__bytes_read.sum + dram__bytes_write.sum of one launch on this
         # workload (profiles/k_step_mixed_coop_poured_bed_1M.txt)
         traffic = TRAFFIC_POURED_BED_1M
+        traffic_source = ("ncu capture of this kernel on this workload (profiles/k_step_mixed_coop_poured_bed_1M.txt); "
+                          "not measured in this run")
     if traffic is None and mixed and args.workload == "channel" and args.model == "hertz_mindlin":
         # (profiles/k_step_mixed_coop_channel_1M.txt), scaled to this launch's spheres
         traffic = TRAFFIC_CHANNEL_PER_SPHERE * stk["n_active"]
+        traffic_source = ("ncu capture on the 1M channel (profiles/k_step_mixed_coop_channel_1M.txt), scaled by "
+                          "the spheres of this launch; not measured in this run")
     reb = int(st1["rebuilds"] - st0["rebuilds"])
     E.close()
     extra = {}
@@ -316,7 +321,7 @@ def run_engine(args):
                         + reb * (11 + sort_launches(sc.n))
                         + int(st1["inner_builds"] - st0["inner_builds"]),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": traffic,
+                     "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_source,
                      "peak_kind": f"{peak_kind} hbm_gbs",
                      "kernel": f"k_step<{'Mixed' if mixed else 'FP64'},{args.model}>", "kernel_ms": k_ms,
                      "algorithmic_bytes": bytes_launch,
@@ -414,6 +419,7 @@ def run_e2e(args, sc, kw):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     E.import_particles(sc, history=sc.history, hist_stride=sc.hist_stride)
+    t_import = time.perf_counter() - t0
     for k in range(steps):
         E.step(1)
         E.export_positions_async(frames[k % 2])
@@ -424,7 +430,8 @@ def run_e2e(args, sc, kw):
     if sc.history is not None:
         h2d += sum(int(np.asarray(a).nbytes) for a in sc.history.values())
     return {"value": n * steps / dt_s, "unit": UNIT, "h2d_bytes_per_step": h2d / steps,
-            "d2h_bytes_per_step": frame.nbytes, "steps": steps}
+            "d2h_bytes_per_step": frame.nbytes, "steps": steps, "import_ms": round(1e3 * t_import, 2),
+            "total_ms": round(1e3 * dt_s, 2)}
 
 
 def active_only(sc):

@@ -52,6 +52,17 @@ struct Arena {
     }
 };
 
+// A host array without value-initialisation (no zero fill before the
+// caller writes every element).
+template <class X>
+struct HostBuf {
+    std::unique_ptr<X[]> p;
+    explicit HostBuf(size_t count) : p(count ? new X[count] : nullptr) {}
+    X* data() { return p.get(); }
+    X& operator[](size_t i) { return p[i]; }
+    const X& operator[](size_t i) const { return p[i]; }
+};
+
 // f(lo, hi) over [0, n) in contiguous chunks, one host thread each (one
 // thread for small n); f must not throw.
 template <class F>
@@ -623,14 +634,16 @@ struct Impl : EngineBase {
                 }
             }
         }
-        std::vector<double4_32a> pos(n);
-        std::vector<V4> vel(n), rot(n), mat(n);
-        std::vector<float4> posh(T::mixed ? n : 0), posl(T::mixed ? n : 0), vl(T::mixed ? n : 0),
+        // staging arrays left uninitialised: the parallel loop below writes
+        // every element (first touch spread over the threads)
+        HostBuf<double4_32a> pos(n);
+        HostBuf<V4> vel(n), rot(n), mat(n);
+        HostBuf<float4> posh(T::mixed ? n : 0), posl(T::mixed ? n : 0), vl(T::mixed ? n : 0),
             wl(T::mixed ? n : 0);
         // only the slot rows some particle uses travel; the device clears the rest
-        std::vector<int> hid((size_t)n * qmax), hwid((size_t)n * qwmax);
-        std::vector<R> hx((size_t)n * qmax), hy((size_t)n * qmax), hz((size_t)n * qmax);
-        std::vector<R> hwx((size_t)n * qwmax), hwy((size_t)n * qwmax), hwz((size_t)n * qwmax);
+        HostBuf<int> hid((size_t)n * qmax), hwid((size_t)n * qwmax);
+        HostBuf<R> hx((size_t)n * qmax), hy((size_t)n * qmax), hz((size_t)n * qmax);
+        HostBuf<R> hwx((size_t)n * qwmax), hwy((size_t)n * qwmax), hwz((size_t)n * qwmax);
         host_parallel_for(n, [&](int lo, int hi) {
             for (int i = lo; i < hi; i++) {
                 const double r = p->r[i];
