@@ -608,31 +608,64 @@ struct Impl : EngineBase {
         const int ntri = mesh ? mesh->ntri : 0;
         int qmax = 0, qwmax = 0;
         double rmax = 0.;
-        for (int i = 0; i < n; i++) {
-            if (rmax < p->r[i]) rmax = p->r[i];
-            if (hist) {
-                nc[i] = p->numCont[i];
-                if (nc[i] < 0) return failv(err, GDEM_ERR_ARG, "import: negative numCont");
-                if (nc[i] > H || nc[i] > p->hist_stride)
-                    return failv(err, GDEM_ERR_CAPACITY, "import: history longer than hist_capacity");
-                if (nc[i] > qmax) qmax = nc[i];
-                for (int q = 0; q < nc[i]; q++) {
-                    const int j = p->indHis[(size_t)i * p->hist_stride + q];
-                    if (j < 0 || j >= n) return failv(err, GDEM_ERR_ARG, "import: history partner id outside [0, n)");
+        // in parallel over contiguous ranges; the first failing range (lowest
+        // particles) decides the error
+        struct Scan {
+            int lo = 0, rc = GDEM_OK, qmax = 0, qwmax = 0;
+            double rmax = 0.;
+            const char* msg = "";
+        };
+        std::vector<Scan> scans;
+        std::mutex scan_mu;
+        host_parallel_for(n, [&](int lo, int hi) {
+            Scan sc;
+            sc.lo = lo;
+            auto bad = [&](int rc, const char* msg) {
+                sc.rc = rc;
+                sc.msg = msg;
+            };
+            for (int i = lo; i < hi && sc.rc == GDEM_OK; i++) {
+                if (sc.rmax < p->r[i]) sc.rmax = p->r[i];
+                if (hist) {
+                    nc[i] = p->numCont[i];
+                    if (nc[i] < 0) { bad(GDEM_ERR_ARG, "import: negative numCont"); break; }
+                    if (nc[i] > H || nc[i] > p->hist_stride) {
+                        bad(GDEM_ERR_CAPACITY, "import: history longer than hist_capacity");
+                        break;
+                    }
+                    if (nc[i] > sc.qmax) sc.qmax = nc[i];
+                    const int* row = p->indHis + (size_t)i * p->hist_stride;
+                    for (int q = 0; q < nc[i]; q++)
+                        if (row[q] < 0 || row[q] >= n) {
+                            bad(GDEM_ERR_ARG, "import: history partner id outside [0, n)");
+                            break;
+                        }
+                }
+                if (histw && sc.rc == GDEM_OK) {
+                    ncw[i] = p->numContWall[i];
+                    if (ncw[i] < 0) { bad(GDEM_ERR_ARG, "import: negative numContWall"); break; }
+                    if (ncw[i] > HW || ncw[i] > p->hist_stride) {
+                        bad(GDEM_ERR_CAPACITY, "import: wall history longer than hist_wall_capacity");
+                        break;
+                    }
+                    if (ncw[i] > sc.qwmax) sc.qwmax = ncw[i];
+                    const int* row = p->indHisWall + (size_t)i * p->hist_stride;
+                    for (int q = 0; q < ncw[i]; q++)
+                        if (row[q] < 0 || row[q] >= ntri) {
+                            bad(GDEM_ERR_ARG, "import: wall history triangle outside the mesh");
+                            break;
+                        }
                 }
             }
-            if (histw) {
-                ncw[i] = p->numContWall[i];
-                if (ncw[i] < 0) return failv(err, GDEM_ERR_ARG, "import: negative numContWall");
-                if (ncw[i] > HW || ncw[i] > p->hist_stride)
-                    return failv(err, GDEM_ERR_CAPACITY, "import: wall history longer than hist_wall_capacity");
-                if (ncw[i] > qwmax) qwmax = ncw[i];
-                for (int q = 0; q < ncw[i]; q++) {
-                    const int t = p->indHisWall[(size_t)i * p->hist_stride + q];
-                    if (t < 0 || t >= ntri)
-                        return failv(err, GDEM_ERR_ARG, "import: wall history triangle outside the mesh");
-                }
-            }
+            std::lock_guard<std::mutex> lock(scan_mu);
+            scans.push_back(sc);
+        });
+        std::sort(scans.begin(), scans.end(), [](const Scan& a, const Scan& b) { return a.lo < b.lo; });
+        for (const Scan& sc : scans) {
+            if (sc.rc != GDEM_OK) return failv(err, sc.rc, sc.msg);
+            qmax = std::max(qmax, sc.qmax);
+            qwmax = std::max(qwmax, sc.qwmax);
+            rmax = std::max(rmax, sc.rmax);
         }
         // staging arrays left uninitialised: the parallel loop below writes
         // every element (first touch spread over the threads)
@@ -689,25 +722,27 @@ struct Impl : EngineBase {
                                         (float)(ww[2] - (double)rot[i].z), 0.f);
                 }
             }
-            // slot rows (slot q of particle i at q * n + i), row by row
-            for (int q = 0; q < qmax; q++)
-                for (int i = lo; i < hi; i++) {
-                    const size_t src = (size_t)i * p->hist_stride + q, dst = (size_t)q * n + i;
+            // slot rows (slot q of particle i at q * n + i): particle by
+            // particle, each reading only its live prefix of the source row
+            for (int i = lo; i < hi; i++) {
+                const size_t row = (size_t)i * p->hist_stride;
+                for (int q = 0; q < qmax; q++) {
+                    const size_t src = row + q, dst = (size_t)q * n + i;
                     const bool on = q < nc[i];
                     hid[dst] = on ? p->indHis[src] : -1;
                     hx[dst] = on ? (R)p->deltHisx[src] : R(0);
                     hy[dst] = on ? (R)p->deltHisy[src] : R(0);
                     hz[dst] = on ? (R)p->deltHisz[src] : R(0);
                 }
-            for (int q = 0; q < qwmax; q++)
-                for (int i = lo; i < hi; i++) {
-                    const size_t src = (size_t)i * p->hist_stride + q, dst = (size_t)q * n + i;
+                for (int q = 0; q < qwmax; q++) {
+                    const size_t src = row + q, dst = (size_t)q * n + i;
                     const bool on = q < ncw[i];
                     hwid[dst] = on ? p->indHisWall[src] : -1;
                     hwx[dst] = on ? (R)p->deltHisxWall[src] : R(0);
                     hwy[dst] = on ? (R)p->deltHisyWall[src] : R(0);
                     hwz[dst] = on ? (R)p->deltHiszWall[src] : R(0);
                 }
+            }
         });
         if (int rc = setup_grid(rmax)) return rc;
         const SBank<T>& S = v.S[0];
