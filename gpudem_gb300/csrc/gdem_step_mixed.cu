@@ -918,11 +918,17 @@ struct __align__(16) CStage {
 };
 static_assert(sizeof(CStage) % 16 == 0, "stage buffers must keep 16-byte alignment");
 
+// The warp's contact queue: a ring the lanes fill kCoopQ contacts each per
+// round and the warp drains 32 at a time (positions grow without bound; the
+// slot of position x is x % kRing).  The queue holds fewer than 32 before a
+// round adds at most 64, so kRing = 96 never overflows.
+constexpr int kRing = 3 * 32;
 struct __align__(16) CQueue {
-    int j[kCoopQ][32];
-    int slot[kCoopQ][32];     // history slot | fresh << 30
-    int who[kCoopQ * 32];     // queue position -> owning lane | its queue row << 8
-    float f[kCoopQ][6][32];   // force and torque of each queued contact
+    int j[kRing];             // partner's storage index
+    int slot[kRing];          // history slot | fresh << 30
+    int who[kRing];           // owning lane
+    float f[6][kRing];        // force and torque of each queued contact
+    unsigned owned[32];       // the positions of a drained batch each lane owns (bit b: head + b)
 };
 
 constexpr size_t kCoopSmem = 2 * kCoopWarps * sizeof(CStage) + kCoopWarps * sizeof(CQueue);
@@ -1092,10 +1098,16 @@ __global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<
                     hit_hi |= (unsigned long long)hit << (k0 - 64);
             }
         }
+        // ---- contacts through the ring: each round every lane queues its
+        // next (up to) Q contacts in row order (partner and history slot);
+        // whenever 32 are queued, or none will follow, the warp computes the
+        // oldest 32 with every lane busy, and each lane adds its own results
+        // in queue order, which is its row order
+        int head = 0, tail = 0;
         while (true) {
-            // ---- the next (up to) Q contacts of this lane, in row order:
-            // their partners and history slots, queued
+            static_assert(Q == 2, "a lane queues at most two contacts per round");
             int cnt = 0;
+            int qj0 = 0, qs0 = 0, qj1 = 0, qs1 = 0;
 #pragma unroll 1
             for (int q = 0; q < Q && (hit_lo | hit_hi) != 0ull; q++) {
                 int k;
@@ -1123,64 +1135,92 @@ __global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<
                     if (rmask != 0xFFFFFFFFu && slot < 63) v.nei[(size_t)k * n + i] = j | ((slot + 1) << kHintShift);
                 }
                 touched |= 1ull << slot;
-                que->j[cnt][lane] = j;
-                que->slot[cnt][lane] = slot | (fresh ? (1 << 30) : 0);
+                if (cnt == 0) {
+                    qj0 = j;
+                    qs0 = slot | (fresh ? (1 << 30) : 0);
+                } else {
+                    qj1 = j;
+                    qs1 = slot | (fresh ? (1 << 30) : 0);
+                }
                 cnt++;
             }
-            // ---- the warp computes every queued contact
             int excl = cnt;
 #pragma unroll
             for (int o2 = 1; o2 < 32; o2 <<= 1) {
                 const int y = __shfl_up_sync(0xffffffffu, excl, o2);
                 if (lane >= o2) excl += y;
             }
-            const int total = __shfl_sync(0xffffffffu, excl, 31);
+            const int added = __shfl_sync(0xffffffffu, excl, 31);
             excl -= cnt;
-            for (int r = 0; r < cnt; r++) que->who[excl + r] = lane | (r << 8);
-            __syncwarp();
-            for (int w = lane; w < total; w += 32) {
-                const int wh = que->who[w];
-                const int ow = wh & 0xff, r = wh >> 8;
-                const int j = que->j[r][ow];
-                const int sl = que->slot[r][ow];
-                const int slot = sl & 0x3fffffff;
-                const int iow = t * 32 + ow;
-                const float4 hiw = S.posh[ow], liw = S.posl[ow], viw = S.vel[ow], wiw = S.rot[ow];
-                const float4 hjq = __ldg(&Aposh[j]), ljq = __ldg(&Aposl[j]);
-                const float4 vj = __ldg(&Avel[j]), wj = __ldg(&Arot[j]);
-                const size_t h = (size_t)slot * n + iow;
-                Vec3<R> sp, cp;
-                if (sl >> 30) {
-                    sp.x = sp.y = sp.z = 0.f;
-                    cp.x = cp.y = cp.z = 0.f;
-                } else {
-                    sp.x = P.hx[h]; sp.y = P.hy[h]; sp.z = P.hz[h];
-                    cp.x = P.cx[h]; cp.y = P.cy[h]; cp.z = P.cz[h];
+            if (cnt > 0) {
+                const int x = (tail + excl) % kRing;
+                que->j[x] = qj0;
+                que->slot[x] = qs0;
+                que->who[x] = lane;
+            }
+            if (cnt > 1) {
+                const int x = (tail + excl + 1) % kRing;
+                que->j[x] = qj1;
+                que->slot[x] = qs1;
+                que->who[x] = lane;
+            }
+            tail += added;
+            const bool more = __any_sync(0xffffffffu, (hit_lo | hit_hi) != 0ull);
+            while (tail - head >= 32 || (!more && tail > head)) {
+                const int B = min(32, tail - head);
+                que->owned[lane] = 0u;
+                __syncwarp();
+                // ---- the warp computes the batch [head, head + B)
+                const int x = (head + lane) % kRing;
+                const int ow = lane < B ? que->who[x] : 32 + lane;
+                if (lane < B) {
+                    const int j = que->j[x];
+                    const int sl = que->slot[x];
+                    const int slot = sl & 0x3fffffff;
+                    const int iow = t * 32 + ow;
+                    const float4 hiw = S.posh[ow], liw = S.posl[ow], viw = S.vel[ow], wiw = S.rot[ow];
+                    const float4 hjq = __ldg(&Aposh[j]), ljq = __ldg(&Aposl[j]);
+                    const float4 vj = __ldg(&Avel[j]), wj = __ldg(&Arot[j]);
+                    const size_t h = (size_t)slot * n + iow;
+                    Vec3<R> sp, cp;
+                    if (sl >> 30) {
+                        sp.x = sp.y = sp.z = 0.f;
+                        cp.x = cp.y = cp.z = 0.f;
+                    } else {
+                        sp.x = P.hx[h]; sp.y = P.hy[h]; sp.z = P.hz[h];
+                        cp.x = P.cx[h]; cp.y = P.cy[h]; cp.z = P.cz[h];
+                    }
+                    const Mat mo = own_material<MODEL>(v, P, iow, hiw.w, viw.w);
+                    const Force6 G = pair_force<MODEL>(v, pair_geometry(hiw, liw, hjq, ljq, per), hiw.w, hjq.w, viw,
+                                                       wiw, vj, wj, viw.w, mo, sp, cp);
+                    P.hx[h] = sp.x; P.hy[h] = sp.y; P.hz[h] = sp.z;
+                    P.cx[h] = cp.x; P.cy[h] = cp.y; P.cz[h] = cp.z;
+                    que->f[0][x] = G.fx;
+                    que->f[1][x] = G.fy;
+                    que->f[2][x] = G.fz;
+                    que->f[3][x] = G.mx;
+                    que->f[4][x] = G.my;
+                    que->f[5][x] = G.mz;
                 }
-                const Mat mo = own_material<MODEL>(v, P, iow, hiw.w, viw.w);
-                const Force6 G = pair_force<MODEL>(v, pair_geometry(hiw, liw, hjq, ljq, per), hiw.w, hjq.w, viw, wiw, vj, wj,
-                                                   viw.w, mo, sp, cp);
-                P.hx[h] = sp.x; P.hy[h] = sp.y; P.hz[h] = sp.z;
-                P.cx[h] = cp.x; P.cy[h] = cp.y; P.cz[h] = cp.z;
-                que->f[r][0][ow] = G.fx;
-                que->f[r][1][ow] = G.fy;
-                que->f[r][2][ow] = G.fz;
-                que->f[r][3][ow] = G.mx;
-                que->f[r][4][ow] = G.my;
-                que->f[r][5][ow] = G.mz;
+                // the batch positions of each owner: one mask per group of
+                // equal owners, written by the group's first lane
+                const unsigned grp = __match_any_sync(0xffffffffu, ow);
+                if (lane < B && (grp & ((1u << lane) - 1u)) == 0u) que->owned[ow] = grp;
+                __syncwarp();
+                // each lane adds its own results in position (row) order
+                for (unsigned m = que->owned[lane]; m != 0u; m &= m - 1u) {
+                    const int y = (head + __ffs((int)m) - 1) % kRing;
+                    F.fx += que->f[0][y];
+                    F.fy += que->f[1][y];
+                    F.fz += que->f[2][y];
+                    F.mx += que->f[3][y];
+                    F.my += que->f[4][y];
+                    F.mz += que->f[5][y];
+                }
+                __syncwarp();
+                head += B;
             }
-            __syncwarp();
-            // each lane adds its own contacts' results in row order
-            for (int r = 0; r < cnt; r++) {
-                F.fx += que->f[r][0][lane];
-                F.fy += que->f[r][1][lane];
-                F.fz += que->f[r][2][lane];
-                F.mx += que->f[r][3][lane];
-                F.my += que->f[r][4][lane];
-                F.mz += que->f[r][5][lane];
-            }
-            __syncwarp();
-            if (!__any_sync(0xffffffffu, (hit_lo | hit_hi) != 0ull)) break;
+            if (!more) break;
         }
         if (active) {
             P.nc[i] = surviving(touched, nc);
