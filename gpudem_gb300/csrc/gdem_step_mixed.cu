@@ -905,8 +905,12 @@ __global__ void __launch_bounds__(kBlock, 2) k_step_mixed_wtma(View<Mixed> v, cu
 // law runs with every lane busy, and its gathers and history loads are in
 // flight together instead of one contact after another.  Shared memory per
 // warp is kept small (two stage buffers and the queue) so that many warps
-// share an SM.
-constexpr int kHidStageRows = 7;
+// share an SM, and so that five CTAs (5 x 38 KB plus the per-CTA reserve)
+// fit the 196 KB shared-memory carveout, leaving 60 KB of each SM's 256 KB
+// to the L1 that the neighbour and history gathers go through: three staged
+// history-key rows measured 0.463 ms on the 1M bed against 0.496 ms with
+// seven (38 + 4 KB per CTA, the 228 KB carveout, 28 KB of L1).
+constexpr int kHidStageRows = 3;
 constexpr int kCoopWarps = 4;
 constexpr int kCoopQ = 2;
 
