@@ -44,7 +44,7 @@ TRAFFIC_POURED_BED_PER_SPHERE = 177_374_720.0 / 300_000
 # bytes per sphere of one step-kernel launch on the periodic channel, from an
 # ncu capture of the 1M-sphere channel (the 10M one is too large to capture);
 # the launch's traffic scales with the spheres it steps
-TRAFFIC_CHANNEL_PER_SPHERE = 247_791_616.0 / 1_000_000
+TRAFFIC_CHANNEL_PER_SPHERE = 230_209_792.0 / 1_000_000
 UNIT = "particle-steps/s"
 METRIC_CHANNEL = "particle-steps/s at 10M spheres in a channel periodic in x, FP32-mixed on 1 GB300"
 
