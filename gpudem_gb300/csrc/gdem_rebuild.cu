@@ -487,10 +487,11 @@ __global__ void k_posf(View<T> v, int gated) {
 // within that band of the cutoff takes the FP64 test.  The decision is the
 // FP64 test's in every case.
 //
-// The row grows in shared memory as partner pIds kept sorted by insertion
-// (slot k of thread t at k * kNbBlock + t: the threads of a warp touch 32
-// banks), and is written out once, mapped back to storage indices through
-// v.where, slot by slot (a warp writes 32 consecutive ints per slot).
+// The row grows in shared memory as partner pIds (slot k of thread t at
+// k * kNbBlock + t: the threads of a warp touch 32 banks), is sorted by
+// insertion once the scan is done, and is written out once, mapped back to
+// storage indices through v.where, slot by slot (a warp writes 32
+// consecutive ints per slot).
 constexpr int kNbBlock = 128;
 constexpr int kNbUnroll = 4;
 
@@ -580,16 +581,7 @@ __global__ void __launch_bounds__(kNbBlock) k_neighbors(View<T> v, int gated) {
                                     overflow = true;
                                     continue;
                                 }
-                                // insertion by pId keeps the row sorted as it grows
-                                const int pid_j = pidv[j];
-                                int k = count;
-                                while (k > 0) {
-                                    const int prev = row[(k - 1) * kNbBlock];
-                                    if (prev < pid_j) break;
-                                    row[k * kNbBlock] = prev;
-                                    k--;
-                                }
-                                row[k * kNbBlock] = pid_j;
+                                row[count * kNbBlock] = pidv[j];  // sorted once the scan is done
                                 count++;
                             }
                         }
@@ -597,6 +589,20 @@ __global__ void __launch_bounds__(kNbBlock) k_neighbors(View<T> v, int gated) {
                 }
             }
             if (overflow || count > v.nei_cap) atomicOr(&ctl->error, 0x1u);
+            // the row by pId: an insertion sort after the scan, run by all the
+            // warp's lanes together rather than one lane per hit during it
+            const int cs = count < CAP ? count : CAP;
+            for (int a = 1; a < cs; a++) {
+                const int key = row[a * kNbBlock];
+                int b = a;
+                while (b > 0) {
+                    const int prev = row[(b - 1) * kNbBlock];
+                    if (prev < key) break;
+                    row[b * kNbBlock] = prev;
+                    b--;
+                }
+                row[b * kNbBlock] = key;
+            }
             const int m = count < v.nei_cap ? count : v.nei_cap;
             for (int k = 0; k < m; k++) v.nei[(size_t)k * n + i] = v.where[row[k * kNbBlock]];
             v.nnei[i] = m;
