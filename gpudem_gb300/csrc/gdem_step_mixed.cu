@@ -898,19 +898,16 @@ __global__ void __launch_bounds__(kBlock, 2) k_step_mixed_wtma(View<Mixed> v, cu
 // The warp-staged pipeline with the particle contacts computed by the whole
 // warp.  Every lane first tests its whole Verlet row (a bit per entry in
 // contact).  Then, kCoopQ contacts per lane at a time, it finds their history
-// slots in row order (the slot search reads the row's first kHidStageRows
-// history keys from shared memory) and queues them; the warp computes the
-// queued contacts 32 at a time, whoever owns them, and each lane adds its
-// own contacts' results back in row order.  The contact
-// law runs with every lane busy, and its gathers and history loads are in
-// flight together instead of one contact after another.  Shared memory per
-// warp is kept small (two stage buffers and the queue) so that many warps
-// share an SM, and so that five CTAs (5 x 38 KB plus the per-CTA reserve)
-// fit the 196 KB shared-memory carveout, leaving 60 KB of each SM's 256 KB
-// to the L1 that the neighbour and history gathers go through: three staged
-// history-key rows measured 0.463 ms on the 1M bed against 0.496 ms with
-// seven (38 + 4 KB per CTA, the 228 KB carveout, 28 KB of L1).
-constexpr int kHidStageRows = 3;
+// slots in row order (the entry's slot hint checked against the key, else a
+// search) and queues them; the warp computes the queued contacts 32 at a
+// time, whoever owns them, and each lane adds its own contacts' results back
+// in row order.  The contact law runs with every lane busy, and its gathers
+// and history loads are in flight together instead of one contact after
+// another.  Shared memory per warp is kept small (two stage buffers and the
+// queue, 7.6 KB) so that five CTAs of four warps share an SM with a large
+// L1 beside them for the neighbour and history gathers: staging the first
+// history-key rows in shared memory as well measured slower (0.463 ms on the
+// 1M bed with three rows, 0.496 with seven, against 0.452 with none).
 constexpr int kCoopWarps = 4;
 constexpr int kCoopQ = 2;
 
@@ -918,7 +915,6 @@ struct __align__(16) CStage {
     float4 posh[32], posl[32], vel[32], rot[32];
     int nnei[32], nneiw[32], nc[32], ncw[32];
     int nei[kNeiStageRows][32];
-    int hid[kHidStageRows][32];
 };
 static_assert(sizeof(CStage) % 16 == 0, "stage buffers must keep 16-byte alignment");
 
@@ -929,9 +925,8 @@ static_assert(sizeof(CStage) % 16 == 0, "stage buffers must keep 16-byte alignme
 constexpr int kRing = 3 * 32;
 struct __align__(16) CQueue {
     int j[kRing];             // partner's storage index
-    int slot[kRing];          // history slot | fresh << 30
-    int who[kRing];           // owning lane
-    float f[6][kRing];        // force and torque of each queued contact
+    int pk[kRing];            // history slot | fresh << 6 | owning lane << 7
+    float f[6][32];           // force and torque of each contact of the batch being drained
     unsigned owned[32];       // the positions of a drained batch each lane owns (bit b: head + b)
 };
 
@@ -942,18 +937,17 @@ __device__ __forceinline__ void bulk_prefetch_l2(const void* src, unsigned bytes
 }
 
 // Bulk copies of sub-tile `t` into `st` (lane 0): positions, velocities,
-// spins and counts, plus the first Verlet rows and history-key rows when
-// every row k*n + 32t starts 16-byte aligned (n a multiple of 4).  The
+// spins and counts, plus the first Verlet rows when every row k*n + 32t
+// starts 16-byte aligned (n a multiple of 4).  The
 // arrays read only at the end of the sub-tile (low parts, reference
 // positions) are prefetched into L2.
 __device__ __forceinline__ void issue_csub(const View<Mixed>& v, const SBank<Mixed>& A, const PBank<Mixed>& P,
-                                           int t, CStage* st, unsigned long long* bar, int nei_rows,
-                                           int hid_rows) {
+                                           int t, CStage* st, unsigned long long* bar, int nei_rows) {
     const int base = t * 32;
     const int cnt = min(32, v.n - base);
     const unsigned b16 = 16u * (unsigned)cnt;
     const unsigned b4 = 4u * (unsigned)((cnt + 3) & ~3);
-    mbar_expect_tx(bar, 4u * b16 + (4u + (unsigned)nei_rows + (unsigned)hid_rows) * b4);
+    mbar_expect_tx(bar, 4u * b16 + (4u + (unsigned)nei_rows) * b4);
     bulk_g2s(st->posh, A.posh + base, b16, bar);
     bulk_g2s(st->posl, A.posl + base, b16, bar);
     bulk_g2s(st->vel, A.vel + base, b16, bar);
@@ -963,30 +957,9 @@ __device__ __forceinline__ void issue_csub(const View<Mixed>& v, const SBank<Mix
     bulk_g2s(st->nc, P.nc + base, b4, bar);
     bulk_g2s(st->ncw, P.ncw + base, b4, bar);
     for (int k = 0; k < nei_rows; k++) bulk_g2s(st->nei[k], v.nei + (size_t)k * v.n + base, b4, bar);
-    for (int k = 0; k < hid_rows; k++) bulk_g2s(st->hid[k], P.hid + (size_t)k * v.n + base, b4, bar);
     bulk_prefetch_l2(A.vell + base, b16);
     bulk_prefetch_l2(A.rotl + base, b16);
     bulk_prefetch_l2(v.refh + base, b16);
-}
-
-// History slot of `key` in row i (find_slot) with the first `rows` keys of
-// the row read from shared memory (hid_s, stride 32).  A new key is written
-// to both copies.
-__device__ __forceinline__ int find_slot_staged(int* hid_s, int rows, int* hid, int n, int i, int& nc, int key,
-                                                int cap, bool& fresh) {
-    for (int q = 0; q < nc; q++) {
-        const int h = q < rows ? hid_s[q * 32] : hid[(size_t)q * n + i];
-        if (h == key) {
-            fresh = false;
-            return q;
-        }
-    }
-    fresh = true;
-    if (nc >= cap) return -1;
-    const int q = nc++;
-    hid[(size_t)q * n + i] = key;
-    if (q < rows) hid_s[q * 32] = key;
-    return q;
 }
 
 template <int MODEL, int WCAP, int MINB, bool PER>
@@ -1012,7 +985,6 @@ __global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<
     const int n = v.n;
     const int nsub = (n + 31) / 32;
     const int nei_rows = (n % 4 == 0) ? min(kNeiStageRows, v.nei_cap) : 0;
-    const int hid_rows = (n % 4 == 0) ? min(kHidStageRows, v.hist_cap) : 0;
     const unsigned rmask = v.row_mask;
     const PerX per = per_of<PER>(v);
     unsigned votes = 0u;
@@ -1028,7 +1000,7 @@ __global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<
     int t = 0;
     if (lane == 0) {
         t = (int)atomicAdd(&ctl->work, 1u);
-        if (t < nsub) issue_csub(v, A, P, t, &stage[0], &full[warp][0], nei_rows, hid_rows);
+        if (t < nsub) issue_csub(v, A, P, t, &stage[0], &full[warp][0], nei_rows);
     }
     t = __shfl_sync(0xffffffffu, t, 0);
     bool timed_out = false;
@@ -1044,7 +1016,7 @@ __global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<
             // the other buffer was last read before the __syncwarp that ended
             // the previous iteration; order those reads before the copy
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            issue_csub(v, A, P, tn, &stage[b ^ 1], &full[warp][b ^ 1], nei_rows, hid_rows);
+            issue_csub(v, A, P, tn, &stage[b ^ 1], &full[warp][b ^ 1], nei_rows);
         }
         const bool ok = mbar_wait_bounded(&full[warp][b], (unsigned)(it >> 1) & 1u, v.wait_tries);
         if (__any_sync(0xffffffffu, !ok)) {
@@ -1069,7 +1041,6 @@ __global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<
         int nc = S.nc[lane];
         unsigned long long touched = 0ull;
         const int nn = active ? S.nnei[lane] : 0;
-        int* hid_s = &S.hid[0][lane];
         const int* nei_s = &S.nei[0][lane];
         // ---- this lane's whole row in one pass, four entries at a time with
         // their gathers in flight together: a bit per row entry in contact
@@ -1128,23 +1099,24 @@ __global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<
                 const int hint = rmask != 0xFFFFFFFFu ? (int)(e >> kHintShift) - 1 : -1;
                 bool fresh = false;
                 int slot;
-                if (hint >= 0 && hint < nc && (hint < hid_rows ? hid_s[hint * 32] : P.hid[(size_t)hint * n + i]) == j) {
+                if (hint >= 0 && hint < nc && P.hid[(size_t)hint * n + i] == j) {
                     slot = hint;
                 } else {
-                    slot = find_slot_staged(hid_s, hid_rows, P.hid, n, i, nc, j, v.hist_cap, fresh);
+                    slot = find_slot<Mixed>(P.hid, n, i, nc, j, v.hist_cap, fresh);
                     if (slot < 0) {
                         err |= 0x4u;
                         continue;
                     }
+                    if (fresh) P.hid[(size_t)slot * n + i] = j;
                     if (rmask != 0xFFFFFFFFu && slot < 63) v.nei[(size_t)k * n + i] = j | ((slot + 1) << kHintShift);
                 }
                 touched |= 1ull << slot;
                 if (cnt == 0) {
                     qj0 = j;
-                    qs0 = slot | (fresh ? (1 << 30) : 0);
+                    qs0 = slot | (fresh ? 64 : 0) | (lane << 7);
                 } else {
                     qj1 = j;
-                    qs1 = slot | (fresh ? (1 << 30) : 0);
+                    qs1 = slot | (fresh ? 64 : 0) | (lane << 7);
                 }
                 cnt++;
             }
@@ -1159,14 +1131,12 @@ __global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<
             if (cnt > 0) {
                 const int x = (tail + excl) % kRing;
                 que->j[x] = qj0;
-                que->slot[x] = qs0;
-                que->who[x] = lane;
+                que->pk[x] = qs0;
             }
             if (cnt > 1) {
                 const int x = (tail + excl + 1) % kRing;
                 que->j[x] = qj1;
-                que->slot[x] = qs1;
-                que->who[x] = lane;
+                que->pk[x] = qs1;
             }
             tail += added;
             const bool more = __any_sync(0xffffffffu, (hit_lo | hit_hi) != 0ull);
@@ -1176,18 +1146,18 @@ __global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<
                 __syncwarp();
                 // ---- the warp computes the batch [head, head + B)
                 const int x = (head + lane) % kRing;
-                const int ow = lane < B ? que->who[x] : 32 + lane;
+                const int sl = lane < B ? que->pk[x] : 0;
+                const int ow = lane < B ? sl >> 7 : 32 + lane;
                 if (lane < B) {
                     const int j = que->j[x];
-                    const int sl = que->slot[x];
-                    const int slot = sl & 0x3fffffff;
+                    const int slot = sl & 63;
                     const int iow = t * 32 + ow;
                     const float4 hiw = S.posh[ow], liw = S.posl[ow], viw = S.vel[ow], wiw = S.rot[ow];
                     const float4 hjq = __ldg(&Aposh[j]), ljq = __ldg(&Aposl[j]);
                     const float4 vj = __ldg(&Avel[j]), wj = __ldg(&Arot[j]);
                     const size_t h = (size_t)slot * n + iow;
                     Vec3<R> sp, cp;
-                    if (sl >> 30) {
+                    if (sl & 64) {
                         sp.x = sp.y = sp.z = 0.f;
                         cp.x = cp.y = cp.z = 0.f;
                     } else {
@@ -1199,12 +1169,12 @@ __global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<
                                                        wiw, vj, wj, viw.w, mo, sp, cp);
                     P.hx[h] = sp.x; P.hy[h] = sp.y; P.hz[h] = sp.z;
                     P.cx[h] = cp.x; P.cy[h] = cp.y; P.cz[h] = cp.z;
-                    que->f[0][x] = G.fx;
-                    que->f[1][x] = G.fy;
-                    que->f[2][x] = G.fz;
-                    que->f[3][x] = G.mx;
-                    que->f[4][x] = G.my;
-                    que->f[5][x] = G.mz;
+                    que->f[0][lane] = G.fx;
+                    que->f[1][lane] = G.fy;
+                    que->f[2][lane] = G.fz;
+                    que->f[3][lane] = G.mx;
+                    que->f[4][lane] = G.my;
+                    que->f[5][lane] = G.mz;
                 }
                 // the batch positions of each owner: one mask per group of
                 // equal owners, written by the group's first lane
@@ -1213,7 +1183,7 @@ __global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<
                 __syncwarp();
                 // each lane adds its own results in position (row) order
                 for (unsigned m = que->owned[lane]; m != 0u; m &= m - 1u) {
-                    const int y = (head + __ffs((int)m) - 1) % kRing;
+                    const int y = __ffs((int)m) - 1;
                     F.fx += que->f[0][y];
                     F.fy += que->f[1][y];
                     F.fz += que->f[2][y];
