@@ -390,13 +390,106 @@ __device__ __forceinline__ void wall_image(const PerX& per, float x0h, float3& p
     }
 }
 
+// Force of one wall contact on particle i (after the feature dedupe), added
+// to F: the normal force, then the history slot of triangle t, the
+// tangential spring, its torque and the rolling resistance
+// (wall_collision_verlet, cpu_dem.cu:238).
+template <int MODEL>
+__device__ __forceinline__ void wall_contact_force(const View<Mixed>& v, const PBank<Mixed>& P, int i, int t,
+                                                   float nx, float ny, float nz, float delmag, float ri, float4 vi,
+                                                   float4 wi, float invmi, const Mat& mt, int& ncw,
+                                                   unsigned long long& wtouched, Force6& F, unsigned& err) {
+    using T = Mixed;
+    using R = float;
+    const int n = v.n;
+    const R vdn = vi.x * nx + vi.y * ny + vi.z * nz;
+    const R vnx = vdn * nx, vny = vdn * ny, vnz = vdn * nz;
+    R fnx, fny, fnz, kt, gt;
+    if (MODEL == 0) {
+        const R eta = mt.etai * mt.sqrtmi;
+        const R fel = mt.ki * delmag;
+        fnx = fel * nx - eta * vnx;
+        fny = fel * ny - eta * vny;
+        fnz = fel * nz - eta * vnz;
+        kt = mt.ki;
+        gt = eta;
+    } else {
+        const R mstar = 1.f / invmi;
+        const R sqrtRd = sqrtf(ri * delmag);
+        const R fel = v.kn_cf * sqrtRd * delmag;
+        const R gn = mt.damp * sqrtf(v.sn_cf * sqrtRd * mstar);
+        const R fnm = fel - gn * vdn;
+        fnx = fnm * nx;
+        fny = fnm * ny;
+        fnz = fnm * nz;
+        kt = v.kt_cf * sqrtRd;
+        gt = mt.damp * sqrtf(kt * mstar);
+    }
+    const R ax_ = ri * wi.x, ay_ = ri * wi.y, az_ = ri * wi.z;
+    const R vtx = (vi.x - vnx) + (ay_ * nz - az_ * ny);
+    const R vty = (vi.y - vny) + (az_ * nx - ax_ * nz);
+    const R vtz = (vi.z - vnz) + (ax_ * ny - ay_ * nx);
+    F.fx += fnx;
+    F.fy += fny;
+    F.fz += fnz;
+    bool fresh;
+    const int slot = find_slot<T>(P.hwid, n, i, ncw, t, v.histw_cap, fresh);
+    if (slot < 0) {
+        err |= 0x8u;
+        return;
+    }
+    const size_t h = (size_t)slot * n + i;
+    Vec3<R> sp, cp;
+    if (fresh) {
+        P.hwid[h] = t;
+        sp.x = sp.y = sp.z = 0.f;
+        cp.x = cp.y = cp.z = 0.f;
+    } else {
+        sp.x = P.hwx[h]; sp.y = P.hwy[h]; sp.z = P.hwz[h];
+        cp.x = P.cwx[h]; cp.y = P.cwy[h]; cp.z = P.cwz[h];
+    }
+    wtouched |= 1ull << slot;
+    Vec3<R> ft;
+    const R fnsq = fnx * fnx + fny * fny + fnz * fnz;
+    tangential<T>(nx, ny, nz, fnsq, vtx, vty, vtz, gt, kt, mt.mu, v.dtf, sp, cp, ft);
+    F.fx += ft.x;
+    F.fy += ft.y;
+    F.fz += ft.z;
+    F.mx += ri * (ny * ft.z - nz * ft.y);
+    F.my += ri * (nz * ft.x - nx * ft.z);
+    F.mz += ri * (nx * ft.y - ny * ft.x);
+    if (MODEL == 1 && v.mu_rollf > 0.f) {
+        const R wn2 = wi.x * wi.x + wi.y * wi.y + wi.z * wi.z;
+        if (wn2 > 0.f) {
+            const R tr = -v.mu_rollf * ri * sqrtf(fnsq) * rsqrtf(wn2);
+            F.mx += tr * wi.x;
+            F.my += tr * wi.y;
+            F.mz += tr * wi.z;
+        }
+    }
+    P.hwx[h] = sp.x; P.hwy[h] = sp.y; P.hwz[h] = sp.z;
+    P.cwx[h] = cp.x; P.cwy[h] = cp.y; P.cwz[h] = cp.z;
+}
+
+// A contact's feature against the features this particle already touched
+// this step: an edge or corner shared by two triangles counts once
+// (wall_collision_verlet's vertex/edge list).  Face contacts (hit -1) always
+// count.
+template <int WCAP>
+__device__ __forceinline__ bool feature_is_new(int hit, int* vore, int& nvore) {
+    if (hit == -1) return true;
+    for (int q = 0; q < nvore; q++)
+        if (vore[q] == hit) return false;
+    if (nvore < WCAP) vore[nvore++] = hit;
+    return true;
+}
+
 // Wall contacts of particle i from its wall list, in list order
 // (wall_collision_verlet, cpu_dem.cu:238), added to f and m.
 template <int MODEL, int WCAP, bool PER>
 __device__ __forceinline__ void wall_forces(const View<Mixed>& v, const PBank<Mixed>& P, int i, int nw, int ncw,
                                             float4 hi, float4 li, float4 vi, float4 wi, float invmi, const Mat& mt,
                                             Force6& F, unsigned& err) {
-    using T = Mixed;
     using R = float;
     const int n = v.n;
     const int* __restrict__ neiw = v.neiw;
@@ -441,84 +534,9 @@ __device__ __forceinline__ void wall_forces(const View<Mixed>& v, const PBank<Mi
             if (!(f.dist < rm)) continue;
             const R delmag = wall_overlap(qh, ql, ri, li.w, v.trif[t], v.trilo[t], f.kind, f.t);
             if (!(delmag > 0.f)) continue;
-        if (f.hit != -1) {
-            bool dup = false;
-            for (int q = 0; q < nvore; q++)
-                if (vore[q] == f.hit) {
-                    dup = true;
-                    break;
-                }
-            if (dup) continue;
-            if (nvore < WCAP) vore[nvore++] = f.hit;
-        }
-        const R nx = f.nx, ny = f.ny, nz = f.nz;
-        const R vdn = vi.x * nx + vi.y * ny + vi.z * nz;
-        const R vnx = vdn * nx, vny = vdn * ny, vnz = vdn * nz;
-        R fnx, fny, fnz, kt, gt;
-        if (MODEL == 0) {
-            const R eta = mt.etai * mt.sqrtmi;
-            const R fel = mt.ki * delmag;
-            fnx = fel * nx - eta * vnx;
-            fny = fel * ny - eta * vny;
-            fnz = fel * nz - eta * vnz;
-            kt = mt.ki;
-            gt = eta;
-        } else {
-            const R mstar = 1.f / invmi;
-            const R sqrtRd = sqrtf(ri * delmag);
-            const R fel = v.kn_cf * sqrtRd * delmag;
-            const R gn = mt.damp * sqrtf(v.sn_cf * sqrtRd * mstar);
-            const R fnm = fel - gn * vdn;
-            fnx = fnm * nx;
-            fny = fnm * ny;
-            fnz = fnm * nz;
-            kt = v.kt_cf * sqrtRd;
-            gt = mt.damp * sqrtf(kt * mstar);
-        }
-        const R ax_ = ri * wi.x, ay_ = ri * wi.y, az_ = ri * wi.z;
-        const R vtx = (vi.x - vnx) + (ay_ * nz - az_ * ny);
-        const R vty = (vi.y - vny) + (az_ * nx - ax_ * nz);
-        const R vtz = (vi.z - vnz) + (ax_ * ny - ay_ * nx);
-        F.fx += fnx;
-        F.fy += fny;
-        F.fz += fnz;
-        bool fresh;
-        const int slot = find_slot<T>(P.hwid, n, i, ncw, t, v.histw_cap, fresh);
-        if (slot < 0) {
-            err |= 0x8u;
-            continue;
-        }
-        const size_t h = (size_t)slot * n + i;
-        Vec3<R> sp, cp;
-        if (fresh) {
-            P.hwid[h] = t;
-            sp.x = sp.y = sp.z = 0.f;
-            cp.x = cp.y = cp.z = 0.f;
-        } else {
-            sp.x = P.hwx[h]; sp.y = P.hwy[h]; sp.z = P.hwz[h];
-            cp.x = P.cwx[h]; cp.y = P.cwy[h]; cp.z = P.cwz[h];
-        }
-        wtouched |= 1ull << slot;
-        Vec3<R> ft;
-        const R fnsq = fnx * fnx + fny * fny + fnz * fnz;
-        tangential<T>(nx, ny, nz, fnsq, vtx, vty, vtz, gt, kt, mt.mu, v.dtf, sp, cp, ft);
-        F.fx += ft.x;
-        F.fy += ft.y;
-        F.fz += ft.z;
-        F.mx += ri * (ny * ft.z - nz * ft.y);
-        F.my += ri * (nz * ft.x - nx * ft.z);
-        F.mz += ri * (nx * ft.y - ny * ft.x);
-        if (MODEL == 1 && v.mu_rollf > 0.f) {
-            const R wn2 = wi.x * wi.x + wi.y * wi.y + wi.z * wi.z;
-            if (wn2 > 0.f) {
-                const R tr = -v.mu_rollf * ri * sqrtf(fnsq) * rsqrtf(wn2);
-                F.mx += tr * wi.x;
-                F.my += tr * wi.y;
-                F.mz += tr * wi.z;
-            }
-        }
-        P.hwx[h] = sp.x; P.hwy[h] = sp.y; P.hwz[h] = sp.z;
-        P.cwx[h] = cp.x; P.cwy[h] = cp.y; P.cwz[h] = cp.z;
+            if (!feature_is_new<WCAP>(f.hit, vore, nvore)) continue;
+            wall_contact_force<MODEL>(v, P, i, t, f.nx, f.ny, f.nz, delmag, ri, vi, wi, invmi, mt, ncw, wtouched, F,
+                                      err);
         }
     }
     P.ncw[i] = surviving(wtouched, ncw);
@@ -962,6 +980,84 @@ __device__ __forceinline__ void issue_csub(const View<Mixed>& v, const SBank<Mix
     bulk_prefetch_l2(v.refh + base, b16);
 }
 
+// The wall contacts of a warp's sub-tile with the geometry spread over the
+// warp: the lanes' wall rows, one after another, are taken 32 candidates at
+// a time, one per lane, through the closest feature and the exact overlap
+// (their record loads in flight together instead of one candidate after
+// another on the few lanes that have any); each lane then takes its own
+// candidates in row order through the feature dedupe and the force, so its
+// sums are those of wall_forces.  The batch results pass through the
+// queue's result buffer.  All lanes call it; nw is 0 on inactive lanes.
+template <int MODEL, int WCAP, bool PER>
+__device__ __forceinline__ void coop_walls(const View<Mixed>& v, const PBank<Mixed>& P, const CStage& S, CQueue* que,
+                                           int t, int lane, bool active, int nw, int ncw, float invmi, const Mat& mt,
+                                           Force6& F, unsigned& err) {
+    const int n = v.n;
+    const PerX per = per_of<PER>(v);
+    int incl = nw;
+#pragma unroll
+    for (int o2 = 1; o2 < 32; o2 <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o2);
+        if (lane >= o2) incl += y;
+    }
+    const int excl = incl - nw;
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    const int i = t * 32 + lane;
+    const float4 hi = S.posh[lane], vi = S.vel[lane], wi = S.rot[lane];
+    unsigned long long wtouched = 0ull;
+    int vore[WCAP];
+    int nvore = 0;
+    for (int base = 0; base < total; base += 32) {
+        const int c = base + lane;
+        // the candidate's owner: the first lane whose running count passes c
+        int ow = 0;
+#pragma unroll
+        for (int step = 16; step >= 1; step >>= 1)
+            if (__shfl_sync(0xffffffffu, incl, ow + step - 1) <= c) ow += step;
+        const int k = c - __shfl_sync(0xffffffffu, excl, ow);
+        int hit = -3, tri = 0;
+        float nx = 0.f, ny = 0.f, nz = 0.f, dm = 0.f;
+        if (c < total) {
+            tri = __ldg(&v.neiw[(size_t)k * n + t * 32 + ow]);
+            const float4 hiw = S.posh[ow], liw = S.posl[ow];
+            const float rm = hiw.w + v.wall_delta;
+            float3 qh = make_float3(hiw.x, hiw.y, hiw.z), ql = make_float3(liw.x, liw.y, liw.z);
+            wall_image(per, v.trif[tri].v0h[0], qh, ql);
+            // beyond rm the plane test inside rejects it, as the prefilter of
+            // wall_forces does
+            const FeatureF f = closest_feature_f(qh, ql, rm * rm, v.trif[tri]);
+            if (f.dist < rm) {
+                const float d = wall_overlap(qh, ql, hiw.w, liw.w, v.trif[tri], v.trilo[tri], f.kind, f.t);
+                if (d > 0.f) {
+                    hit = f.hit;
+                    nx = f.nx;
+                    ny = f.ny;
+                    nz = f.nz;
+                    dm = d;
+                }
+            }
+        }
+        que->f[0][lane] = nx;
+        que->f[1][lane] = ny;
+        que->f[2][lane] = nz;
+        que->f[3][lane] = dm;
+        que->f[4][lane] = __int_as_float(hit);
+        que->f[5][lane] = __int_as_float(tri);
+        __syncwarp();
+        // this lane's candidates in the batch, in row order
+        const int y1 = min(incl, base + 32) - base;
+        for (int y = max(excl, base) - base; y < y1; y++) {
+            const int fh = __float_as_int(que->f[4][y]);
+            if (fh == -3) continue;
+            if (!feature_is_new<WCAP>(fh, vore, nvore)) continue;
+            wall_contact_force<MODEL>(v, P, i, __float_as_int(que->f[5][y]), que->f[0][y], que->f[1][y],
+                                      que->f[2][y], que->f[3][y], hi.w, vi, wi, invmi, mt, ncw, wtouched, F, err);
+        }
+        __syncwarp();
+    }
+    if (active) P.ncw[i] = surviving(wtouched, ncw);
+}
+
 template <int MODEL, int WCAP, int MINB, bool PER>
 __global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<Mixed> v, cudaGraphConditionalHandle cond, cudaGraphConditionalHandle cond_inner,
                                                                     int use_cond) {
@@ -1196,6 +1292,12 @@ __global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<
             }
             if (!more) break;
         }
+        // ---- wall contacts, the geometry over the whole warp
+        const R invmi = S.vel[lane].w;
+        Mat mt = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        if (active) mt = own_material<MODEL>(v, P, i, S.posh[lane].w, invmi);
+        coop_walls<MODEL, WCAP, PER>(v, P, S, que, t, lane, active, active ? S.nneiw[lane] : 0, S.ncw[lane], invmi, mt,
+                                     F, err);
         if (active) {
             P.nc[i] = surviving(touched, nc);
             Own o;
@@ -1203,9 +1305,6 @@ __global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<
             o.hi = S.posh[lane];
             o.li = S.posl[lane];
             o.vi = S.vel[lane];
-            const R invmi = o.vi.w;
-            const Mat mt = own_material<MODEL>(v, P, i, o.hi.w, invmi);
-            wall_forces<MODEL, WCAP, PER>(v, P, i, S.nneiw[lane], S.ncw[lane], o.hi, o.li, o.vi, o.wi, invmi, mt, F, err);
             o.vl = __ldg(&A.vell[i]);
             o.wl = __ldg(&A.rotl[i]);
             o.rh = __ldg(&v.refh[i]);
