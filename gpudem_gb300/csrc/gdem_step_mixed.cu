@@ -928,6 +928,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_step_mixed_wtma(View<Mixed> v, cu
 // 1M bed with three rows, 0.496 with seven, against 0.452 with none).
 constexpr int kCoopWarps = 4;
 constexpr int kCoopQ = 2;
+constexpr int kRowUnroll = 4;
 
 struct __align__(16) CStage {
     float4 posh[32], posl[32], vel[32], rot[32];
@@ -1138,27 +1139,29 @@ __global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<
         unsigned long long touched = 0ull;
         const int nn = active ? S.nnei[lane] : 0;
         const int* nei_s = &S.nei[0][lane];
-        // ---- this lane's whole row in one pass, four entries at a time with
-        // their gathers in flight together: a bit per row entry in contact
+        // ---- this lane's whole row in one pass, kRowUnroll entries at a time
+        // with their gathers in flight together: a bit per row entry in contact
         unsigned long long hit_lo = 0ull, hit_hi = 0ull;
         {
+            constexpr int U = kRowUnroll;
+            static_assert(64 % U == 0, "a group of row entries stays within one 64-bit hit mask");
             const float4 hi = S.posh[lane], li = S.posl[lane];
             const float delta = v.nb_delta;
-            for (int k0 = 0; k0 < nn; k0 += 4) {
-                int jj[4];
+            for (int k0 = 0; k0 < nn; k0 += U) {
+                int jj[U];
 #pragma unroll
-                for (int q = 0; q < 4; q++) {
+                for (int q = 0; q < U; q++) {
                     const int k = k0 + q;
                     jj[q] = k < nn ? (int)((unsigned)(k < nei_rows ? nei_s[k * 32] : __ldg(&nei[(size_t)k * n + i])) & rmask)
                                    : -1;
                 }
-                float4 hj[4];
+                float4 hj[U];
 #pragma unroll
-                for (int q = 0; q < 4; q++)
+                for (int q = 0; q < U; q++)
                     if (jj[q] >= 0) hj[q] = __ldg(&Aposh[jj[q]]);
                 unsigned hit = 0u;
 #pragma unroll
-                for (int q = 0; q < 4; q++) {
+                for (int q = 0; q < U; q++) {
                     if (jj[q] < 0) continue;
                     const int h = contact_hint(hi, hj[q], delta, per);
                     if (h > 0 || (h < 0 && exact_contact(hi, li, hj[q], __ldg(&Aposl[jj[q]]), per))) hit |= 1u << q;
