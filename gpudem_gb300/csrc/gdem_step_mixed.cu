@@ -922,16 +922,16 @@ __global__ void __launch_bounds__(kBlock, 2) k_step_mixed_wtma(View<Mixed> v, cu
 // in row order.  The contact law runs with every lane busy, and its gathers
 // and history loads are in flight together instead of one contact after
 // another.  Shared memory per warp is kept small (two stage buffers and the
-// queue, 5.9 KB) so that five CTAs of four warps share an SM with a large
+// queue, 6.9 KB) so that five CTAs of four warps share an SM with a large
 // L1 beside them for the neighbour and history gathers: staging the first
 // history-key rows in shared memory as well measured slower (0.463 ms on the
 // 1M bed with three rows, 0.496 with seven, against 0.452 with none).
 constexpr int kCoopWarps = 4;
 constexpr int kCoopQ = 2;
-constexpr int kRowUnroll = 4;
 
 struct __align__(16) CStage {
     float4 posh[32], posl[32], vel[32], rot[32];
+    int nnei[32], nneiw[32], nc[32], ncw[32];
     int nei[kNeiStageRows][32];
 };
 static_assert(sizeof(CStage) % 16 == 0, "stage buffers must keep 16-byte alignment");
@@ -954,9 +954,9 @@ __device__ __forceinline__ void bulk_prefetch_l2(const void* src, unsigned bytes
     asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
 }
 
-// Bulk copies of sub-tile `t` into `st` (lane 0): positions, velocities and
-// spins, plus the first Verlet rows when every row k*n + 32t starts 16-byte
-// aligned (n a multiple of 4).  The
+// Bulk copies of sub-tile `t` into `st` (lane 0): positions, velocities,
+// spins and counts, plus the first Verlet rows when every row k*n + 32t
+// starts 16-byte aligned (n a multiple of 4).  The
 // arrays read only at the end of the sub-tile (low parts, reference
 // positions) are prefetched into L2.
 __device__ __forceinline__ void issue_csub(const View<Mixed>& v, const SBank<Mixed>& A, const PBank<Mixed>& P,
@@ -965,11 +965,15 @@ __device__ __forceinline__ void issue_csub(const View<Mixed>& v, const SBank<Mix
     const int cnt = min(32, v.n - base);
     const unsigned b16 = 16u * (unsigned)cnt;
     const unsigned b4 = 4u * (unsigned)((cnt + 3) & ~3);
-    mbar_expect_tx(bar, 4u * b16 + (unsigned)nei_rows * b4);
+    mbar_expect_tx(bar, 4u * b16 + (4u + (unsigned)nei_rows) * b4);
     bulk_g2s(st->posh, A.posh + base, b16, bar);
     bulk_g2s(st->posl, A.posl + base, b16, bar);
     bulk_g2s(st->vel, A.vel + base, b16, bar);
     bulk_g2s(st->rot, A.rot + base, b16, bar);
+    bulk_g2s(st->nnei, v.nnei + base, b4, bar);
+    bulk_g2s(st->nneiw, v.nneiw + base, b4, bar);
+    bulk_g2s(st->nc, P.nc + base, b4, bar);
+    bulk_g2s(st->ncw, P.ncw + base, b4, bar);
     for (int k = 0; k < nei_rows; k++) bulk_g2s(st->nei[k], v.nei + (size_t)k * v.n + base, b4, bar);
     bulk_prefetch_l2(A.vell + base, b16);
     bulk_prefetch_l2(A.rotl + base, b16);
@@ -1110,17 +1114,6 @@ __global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             issue_csub(v, A, P, tn, &stage[b ^ 1], &full[warp][b ^ 1], nei_rows);
         }
-        // the counts come straight from HBM (coalesced, in flight during the
-        // wait): staging them too made each CTA 4 KB larger, enough to move the
-        // shared-memory carveout a step up and shrink the L1
-        int c_nn = 0, c_nw = 0, c_nc = 0, c_ncw = 0;
-        if (t * 32 + lane < n) {
-            const int ii = t * 32 + lane;
-            c_nn = __ldg(&v.nnei[ii]);
-            c_nw = __ldg(&v.nneiw[ii]);
-            c_nc = P.nc[ii];
-            c_ncw = P.ncw[ii];
-        }
         const bool ok = mbar_wait_bounded(&full[warp][b], (unsigned)(it >> 1) & 1u, v.wait_tries);
         if (__any_sync(0xffffffffu, !ok)) {
             timed_out = true;
@@ -1141,33 +1134,31 @@ __global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<
             freeze_one(v, B, i, o);
         }
         Force6 F = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-        int nc = c_nc;
+        int nc = S.nc[lane];
         unsigned long long touched = 0ull;
-        const int nn = active ? c_nn : 0;
+        const int nn = active ? S.nnei[lane] : 0;
         const int* nei_s = &S.nei[0][lane];
-        // ---- this lane's whole row in one pass, kRowUnroll entries at a time
-        // with their gathers in flight together: a bit per row entry in contact
+        // ---- this lane's whole row in one pass, four entries at a time with
+        // their gathers in flight together: a bit per row entry in contact
         unsigned long long hit_lo = 0ull, hit_hi = 0ull;
         {
-            constexpr int U = kRowUnroll;
-            static_assert(64 % U == 0, "a group of row entries stays within one 64-bit hit mask");
             const float4 hi = S.posh[lane], li = S.posl[lane];
             const float delta = v.nb_delta;
-            for (int k0 = 0; k0 < nn; k0 += U) {
-                int jj[U];
+            for (int k0 = 0; k0 < nn; k0 += 4) {
+                int jj[4];
 #pragma unroll
-                for (int q = 0; q < U; q++) {
+                for (int q = 0; q < 4; q++) {
                     const int k = k0 + q;
                     jj[q] = k < nn ? (int)((unsigned)(k < nei_rows ? nei_s[k * 32] : __ldg(&nei[(size_t)k * n + i])) & rmask)
                                    : -1;
                 }
-                float4 hj[U];
+                float4 hj[4];
 #pragma unroll
-                for (int q = 0; q < U; q++)
+                for (int q = 0; q < 4; q++)
                     if (jj[q] >= 0) hj[q] = __ldg(&Aposh[jj[q]]);
                 unsigned hit = 0u;
 #pragma unroll
-                for (int q = 0; q < U; q++) {
+                for (int q = 0; q < 4; q++) {
                     if (jj[q] < 0) continue;
                     const int h = contact_hint(hi, hj[q], delta, per);
                     if (h > 0 || (h < 0 && exact_contact(hi, li, hj[q], __ldg(&Aposl[jj[q]]), per))) hit |= 1u << q;
@@ -1305,7 +1296,7 @@ __global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<
         const R invmi = S.vel[lane].w;
         Mat mt = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         if (active) mt = own_material<MODEL>(v, P, i, S.posh[lane].w, invmi);
-        coop_walls<MODEL, WCAP, PER>(v, P, S, que, t, lane, active, active ? c_nw : 0, c_ncw, invmi, mt,
+        coop_walls<MODEL, WCAP, PER>(v, P, S, que, t, lane, active, active ? S.nneiw[lane] : 0, S.ncw[lane], invmi, mt,
                                      F, err);
         if (active) {
             P.nc[i] = surviving(touched, nc);
