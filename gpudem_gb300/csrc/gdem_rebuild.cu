@@ -939,6 +939,9 @@ __global__ void __launch_bounds__(kBlock) k_wall_lists(View<T> v, int gated) {
 // skin, when the step asks for new rows (ctl->irefresh); every list rebuild
 // asks too.  Gated on that request in every launch mode.
 constexpr int kInnerKeys = 8;
+// row entries in flight per thread: 4 measured 180 us on the 1M bed, 8 and 16
+// (more registers, fewer resident warps) 207 and 277 us
+constexpr int kInnerUnroll = 4;
 
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_inner(View<T> v) {
@@ -962,17 +965,17 @@ __global__ void __launch_bounds__(kBlock) k_inner(View<T> v) {
                 int hk[kInnerKeys];
 #pragma unroll
                 for (int q = 0; q < kInnerKeys; q++) hk[q] = q < nc ? P.hid[(size_t)q * n + i] : -1;
-                // four row entries at a time, their gathers in flight together
-                for (int k0 = 0; k0 < nn; k0 += 4) {
-                    int jj[4];
-                    float4 hj[4];
+                // kInnerUnroll row entries at a time, their gathers in flight together
+                for (int k0 = 0; k0 < nn; k0 += kInnerUnroll) {
+                    int jj[kInnerUnroll];
+                    float4 hj[kInnerUnroll];
 #pragma unroll
-                    for (int u = 0; u < 4; u++) jj[u] = k0 + u < nn ? v.nei[(size_t)(k0 + u) * n + i] : -1;
+                    for (int u = 0; u < kInnerUnroll; u++) jj[u] = k0 + u < nn ? v.nei[(size_t)(k0 + u) * n + i] : -1;
 #pragma unroll
-                    for (int u = 0; u < 4; u++)
+                    for (int u = 0; u < kInnerUnroll; u++)
                         if (jj[u] >= 0) hj[u] = S.posh[jj[u]];
 #pragma unroll
-                    for (int u = 0; u < 4; u++) {
+                    for (int u = 0; u < kInnerUnroll; u++) {
                         const int j = jj[u];
                         if (j < 0 || !(hj[u].w > 0.f)) continue;  // inactive for good
                         const float dx = image_dxf(v, hi.x - hj[u].x), dy = hi.y - hj[u].y, dz = hi.z - hj[u].z;
