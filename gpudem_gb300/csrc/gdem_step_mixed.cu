@@ -958,7 +958,7 @@ __device__ __forceinline__ void bulk_prefetch_l2(const void* src, unsigned bytes
 // spins and counts, plus the first Verlet rows when every row k*n + 32t
 // starts 16-byte aligned (n a multiple of 4).  The
 // arrays read only at the end of the sub-tile (low parts, reference
-// positions) are prefetched into L2.
+// positions of the list and inner rows) are prefetched into L2.
 __device__ __forceinline__ void issue_csub(const View<Mixed>& v, const SBank<Mixed>& A, const PBank<Mixed>& P,
                                            int t, CStage* st, unsigned long long* bar, int nei_rows) {
     const int base = t * 32;
@@ -978,6 +978,7 @@ __device__ __forceinline__ void issue_csub(const View<Mixed>& v, const SBank<Mix
     bulk_prefetch_l2(A.vell + base, b16);
     bulk_prefetch_l2(A.rotl + base, b16);
     bulk_prefetch_l2(v.refh + base, b16);
+    if (v.inner_on) bulk_prefetch_l2(v.refi + base, b16);
 }
 
 // The wall contacts of a warp's sub-tile with the geometry spread over the
