@@ -988,11 +988,13 @@ __device__ __forceinline__ void issue_csub(const View<Mixed>& v, const SBank<Mix
 // another on the few lanes that have any); each lane then takes its own
 // candidates in row order through the feature dedupe and the force, so its
 // sums are those of wall_forces.  The batch results pass through the
-// queue's result buffer.  All lanes call it; nw is 0 on inactive lanes.
+// queue's result buffer.  A lane's own state and material are read only
+// where it has a contact, so none of it is held in registers across the
+// geometry (which removed the kernel's register spills).  All lanes call it;
+// nw is 0 on inactive lanes.
 template <int MODEL, int WCAP, bool PER>
 __device__ __forceinline__ void coop_walls(const View<Mixed>& v, const PBank<Mixed>& P, const CStage& S, CQueue* que,
-                                           int t, int lane, bool active, int nw, int ncw, float invmi, const Mat& mt,
-                                           Force6& F, unsigned& err) {
+                                           int t, int lane, bool active, int nw, int ncw, Force6& F, unsigned& err) {
     const int n = v.n;
     const PerX per = per_of<PER>(v);
     int incl = nw;
@@ -1004,7 +1006,6 @@ __device__ __forceinline__ void coop_walls(const View<Mixed>& v, const PBank<Mix
     const int excl = incl - nw;
     const int total = __shfl_sync(0xffffffffu, incl, 31);
     const int i = t * 32 + lane;
-    const float4 hi = S.posh[lane], vi = S.vel[lane], wi = S.rot[lane];
     unsigned long long wtouched = 0ull;
     int vore[WCAP];
     int nvore = 0;
@@ -1051,8 +1052,11 @@ __device__ __forceinline__ void coop_walls(const View<Mixed>& v, const PBank<Mix
             const int fh = __float_as_int(que->f[4][y]);
             if (fh == -3) continue;
             if (!feature_is_new<WCAP>(fh, vore, nvore)) continue;
+            // this lane's state and material, read only where it has a contact
+            const float4 hi = S.posh[lane], vi = S.vel[lane], wi = S.rot[lane];
+            const Mat mt = own_material<MODEL>(v, P, i, hi.w, vi.w);
             wall_contact_force<MODEL>(v, P, i, __float_as_int(que->f[5][y]), que->f[0][y], que->f[1][y],
-                                      que->f[2][y], que->f[3][y], hi.w, vi, wi, invmi, mt, ncw, wtouched, F, err);
+                                      que->f[2][y], que->f[3][y], hi.w, vi, wi, vi.w, mt, ncw, wtouched, F, err);
         }
         __syncwarp();
     }
@@ -1294,12 +1298,9 @@ __global__ void __launch_bounds__(kCoopWarps * 32, MINB) k_step_mixed_coop(View<
             if (!more) break;
         }
         // ---- wall contacts, the geometry over the whole warp
-        const R invmi = S.vel[lane].w;
-        Mat mt = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-        if (active) mt = own_material<MODEL>(v, P, i, S.posh[lane].w, invmi);
-        coop_walls<MODEL, WCAP, PER>(v, P, S, que, t, lane, active, active ? S.nneiw[lane] : 0, S.ncw[lane], invmi, mt,
-                                     F, err);
+        coop_walls<MODEL, WCAP, PER>(v, P, S, que, t, lane, active, active ? S.nneiw[lane] : 0, S.ncw[lane], F, err);
         if (active) {
+            const Mat mt = own_material<MODEL>(v, P, i, S.posh[lane].w, S.vel[lane].w);
             P.nc[i] = surviving(touched, nc);
             Own o;
             o.wi = S.rot[lane];
