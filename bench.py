@@ -40,11 +40,11 @@ METRIC = "particle-steps/s at 1M spheres, FP32-mixed vs FP64 plain on 1 GB300 (e
 # DRAM bytes (read + write) per sphere of one step-kernel launch on the poured
 # chute bed, from an ncu capture at 300k spheres (the 1M bed is too large to
 # capture with --set full); scaled by the spheres of a launch
-TRAFFIC_POURED_BED_PER_SPHERE = 182_386_432.0 / 300_000
+TRAFFIC_POURED_BED_PER_SPHERE = 181_997_312.0 / 300_000
 # bytes per sphere of one step-kernel launch on the periodic channel, from an
 # ncu capture of the 1M-sphere channel (the 10M one is too large to capture);
 # the launch's traffic scales with the spheres it steps
-TRAFFIC_CHANNEL_PER_SPHERE = 217_718_528.0 / 1_000_000
+TRAFFIC_CHANNEL_PER_SPHERE = 218_407_936.0 / 1_000_000
 UNIT = "particle-steps/s"
 METRIC_CHANNEL = "particle-steps/s at 10M spheres in a channel periodic in x, FP32-mixed on 1 GB300"
 
