@@ -37,10 +37,11 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "particle-steps/s at 1M spheres, FP32-mixed vs FP64 plain on 1 GB300 (err≤1e-4·r_min)"
-# DRAM bytes (read + write) per sphere of one step-kernel launch on the poured
-# chute bed, from an ncu capture at 300k spheres (the 1M bed is too large to
-# capture with --set full); scaled by the spheres of a launch
-TRAFFIC_POURED_BED_PER_SPHERE = 181_997_312.0 / 300_000
+# DRAM bytes (read + write) per sphere of one step-kernel launch on the 1M
+# poured chute bed, from a one-pass ncu capture of the DRAM byte counters on
+# that launch itself (profiles/k_step_mixed_coop_poured_bed_1M_dram.txt);
+# scaled by the spheres of a launch
+TRAFFIC_POURED_BED_PER_SPHERE = 758_400_000.0 / 999_999
 # bytes per sphere of one step-kernel launch on the periodic channel, from an
 # ncu capture of the 1M-sphere channel (the 10M one is too large to capture);
 # the launch's traffic scales with the spheres it steps
@@ -262,10 +263,11 @@ def run_engine(args):
     traffic_source = "--traffic" if traffic is not None else None
     if traffic is None and mixed and args.workload == "poured" and args.model == "hertz_mindlin":
         # dram__bytes_read.sum + dram__bytes_write.sum per sphere of one launch
-        # on the 300k bed (profiles/k_step_mixed_coop_poured_bed_300k.txt)
+        # on the 1M bed (profiles/k_step_mixed_coop_poured_bed_1M_dram.txt)
         traffic = TRAFFIC_POURED_BED_PER_SPHERE * stk["n_active"]
-        traffic_source = ("ncu capture on the 300k-sphere bed (profiles/k_step_mixed_coop_poured_bed_300k.txt), "
-                          "scaled by the spheres of this launch; not measured in this run")
+        traffic_source = ("one-pass ncu capture of the DRAM counters on the 1M bed "
+                          "(profiles/k_step_mixed_coop_poured_bed_1M_dram.txt), per sphere times the spheres of "
+                          "this launch; not measured in this run")
     if traffic is None and mixed and args.workload == "channel" and args.model == "hertz_mindlin":
         # (profiles/k_step_mixed_coop_channel_1M.txt), scaled to this launch's spheres
         traffic = TRAFFIC_CHANNEL_PER_SPHERE * stk["n_active"]
